@@ -1,0 +1,167 @@
+/*
+ * qgb300.h — C ABI of the GB300 (sm_103a) state-vector engine behind the
+ * qibo backend plugin ``qibo_gb300``.
+ *
+ * The reference (qibo 0.3.5) is pure Python and has no FFI of its own; its
+ * backend interface is the Python class ``qibo.backends.abstract.Backend``.
+ * Each entry point below states which reference method it replaces
+ * (paths relative to the reference's ``src/qibo/``).  A Python, C or C++
+ * host binds these symbols with plain pointers and sizes (ctypes in
+ * ``qibo_gb300/_lib.py``).
+ *
+ * Conventions
+ *  - Every function returns an int status: QGB_OK (0) or one of the
+ *    QGB_ERR_* codes; ``qgb_last_error()`` gives the message of the last
+ *    failure on the calling host thread.
+ *  - A state is a device buffer of 2^nqubits interleaved complex amplitudes:
+ *    QGB_C128 = 2 x double (16 B), QGB_C64 = 2 x float (8 B), allocated with
+ *    ``qgb_malloc`` (or any cudaMalloc'ed buffer with 256-byte alignment).
+ *  - Qubit numbering is qibo's: qubit 0 is the most significant bit of the
+ *    amplitude index (backends/abstract.py:2327-2355), i.e. qubit q has
+ *    stride 2^(nqubits-1-q).
+ *  - Gate matrices are host arrays of 2*4^k doubles (re, im interleaved,
+ *    row-major, rows = outputs), whose index bits follow the order of the
+ *    ``qubits`` array: qubits[0] is the most significant matrix-index bit
+ *    (the reference's ``matrix @ state`` after moving ``gate.qubits`` to the
+ *    front, backends/abstract.py:2350-2355).  Matrices travel by value in the
+ *    kernel parameters: no device allocation, no host-device copy.
+ *  - ``stream`` is a cudaStream_t (NULL = legacy default stream).  All
+ *    calls are asynchronous and stream-ordered unless stated otherwise.
+ */
+#ifndef QGB300_H
+#define QGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGB_OK 0
+#define QGB_ERR_INVALID 1     /* bad argument (qubit out of range, size, dtype) */
+#define QGB_ERR_OOM 2         /* device allocation failed (backends/abstract.py:2500-2510) */
+#define QGB_ERR_CUDA 3        /* any other CUDA runtime error */
+#define QGB_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define QGB_ERR_UNSUPPORTED 5 /* valid request this build does not handle */
+
+#define QGB_C64 0
+#define QGB_C128 1
+
+/* ---- library / device ------------------------------------------------- */
+const char* qgb_last_error(void);
+int qgb_version(void);
+/* Number of kernels this library has launched in the process so far. */
+int64_t qgb_launch_count(void);
+/* Select the device and report its SM count. */
+int qgb_device_init(int device, int* sm_count);
+int qgb_mem_info(size_t* free_bytes, size_t* total_bytes);
+int qgb_malloc(void** ptr, size_t bytes);              /* OOM -> QGB_ERR_OOM */
+int qgb_free(void* ptr);
+int qgb_memcpy_h2d(void* dst, const void* src, size_t bytes, void* stream);
+int qgb_memcpy_d2h(void* dst, const void* src, size_t bytes, void* stream);
+int qgb_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
+int qgb_memset_zero(void* ptr, size_t bytes, void* stream);
+int qgb_stream_sync(void* stream);
+
+/* ---- state creation: Backend.zero_state (backends/abstract.py:2243-2273),
+ *      NumpyBackend.cast (backends/numpy.py:38-64) ----------------------- */
+int qgb_state_zero(void* state, int nqubits, int dtype, void* stream);
+int qgb_state_basis(void* state, int nqubits, int dtype, int64_t index, void* stream);
+/* dst = src converted between QGB_C128 and QGB_C64 (same n). */
+int qgb_state_cast(const void* src, int src_dtype, void* dst, int dst_dtype, int nqubits, void* stream);
+/* state *= scale (real); used for renormalisation. */
+int qgb_state_scale(void* state, int nqubits, int dtype, double scale, void* stream);
+
+/* ---- gate application: Backend.apply_gate (backends/abstract.py:2322-2361)
+ *      and Backend._apply_gate_controlled_by (:3176-3197) ---------------- */
+/* Apply the 2^k x 2^k ``matrix`` on ``qubits[0..k)`` (k <= 5), active only
+ * where every qubit in ``controls[0..ncontrols)`` is 1 (ncontrols may be 0).
+ * The engine classifies the matrix (hidden controls, diagonal, permutation
+ * with phases, dense) and launches the matching kernel. */
+int qgb_apply_gate(void* state, int nqubits, int dtype, const int* qubits, int k,
+                   const int* controls, int ncontrols, const double* matrix, void* stream);
+/* Specialised entry points (no classification).  Dense 2x2 on ``target``. */
+int qgb_apply_1q(void* state, int nqubits, int dtype, int target, const double* matrix, void* stream);
+/* Dense 4x4 on (q0, q1); q0 is the most significant matrix bit. */
+int qgb_apply_2q(void* state, int nqubits, int dtype, int q0, int q1, const double* matrix, void* stream);
+/* Multiply by phase (re, im) every amplitude whose qubits[0..nq) are all 1
+ * (CZ, CU1, CCZ, Z, S, T, U1 after control extraction). */
+int qgb_apply_phase(void* state, int nqubits, int dtype, const int* qubits, int nq,
+                    double phase_re, double phase_im, void* stream);
+/* SWAP (models/qft.py:56-58 uses it), optionally controlled. */
+int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1,
+                   const int* controls, int ncontrols, void* stream);
+
+/* Apply a whole gate list (a circuit, or a fused block sequence) in order.
+ * ``ops`` is an array of ``nops`` qgb_op records, ``coefs`` holds their
+ * matrices (each op's ``coef_offset`` indexes doubles).  The engine plans
+ * shared-memory passes that apply many gates per read+write of the state
+ * when ``flags & QGB_PLAN_BLOCKED``, otherwise it runs gate by gate. */
+typedef struct qgb_op {
+    int32_t k;              /* number of gate qubits (<= 5) */
+    int32_t ncontrols;      /* number of controls (<= 8) */
+    int32_t qubits[5];      /* gate qubits, most significant matrix bit first */
+    int32_t controls[8];
+    int64_t coef_offset;    /* offset (in doubles) of the 2*4^k matrix in coefs */
+} qgb_op;
+#define QGB_PLAN_BLOCKED 1
+int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
+                      const double* coefs, int flags, void* stream);
+
+/* ---- measurement: Backend.calculate_probabilities (:2734-2758,
+ *      _order_probabilities :3371-3381), sample_shots / sample_frequencies
+ *      (:2760-2801) --------------------------------------------------------- */
+/* out[2^nq] (device, float64) = marginal probabilities of qubits[0..nq) in
+ * the given order (qubits[0] is the most significant output bit),
+ * accumulated in FP64.  ``scratch`` is a device buffer of at least
+ * qgb_probs_scratch_bytes(nqubits, nq) bytes (may be NULL when that is 0). */
+size_t qgb_probs_scratch_bytes(int nqubits, int nq);
+int qgb_probabilities(const void* state, int nqubits, int dtype, const int* qubits, int nq,
+                      double* out, void* scratch, void* stream);
+/* Sum of |psi|^2 in FP64 written to *out (device pointer); ``scratch`` is a
+ * device buffer of qgb_norm_scratch_bytes() bytes. */
+size_t qgb_norm_scratch_bytes(void);
+int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scratch, void* stream);
+/* Draw ``nshots`` outcomes from the (unnormalised) FP64 distribution
+ * probs[0..2^m) with a Philox4x32-10 stream keyed by ``seed``; the CDF is an
+ * FP64 prefix sum built in ``scratch`` (qgb_sample_scratch_bytes).  Writes
+ * either samples[nshots] (int64, outcome index) or counts[2^m] (int64
+ * histogram), whichever pointer is non-NULL (device pointers). */
+size_t qgb_sample_scratch_bytes(int m);
+int qgb_sample(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
+               int64_t* counts, void* scratch, void* stream);
+/* Raw Philox4x32-10 words: out[4t+e] = word e of philox(counter = (t_lo,
+ * t_hi, c2, c3), key = (k0, k1)), t < n4 (device buffer).  Exposes the
+ * generator behind qgb_sample for known-answer tests. */
+int qgb_philox_fill(uint32_t* out, int64_t n4, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                    void* stream);
+
+/* ---- expectation values: Backend.exp_value_observable_symbolic
+ *      (backends/abstract.py:2946-3054) ------------------------------------ */
+/* out (device, float64) = sum_t coef[t] * <psi| P_t |psi> for Pauli strings
+ * given as bit masks over qibo qubits (bit q of the mask = qubit q):
+ * xmask = qubits carrying X or Y, zmask = qubits carrying Z or Y.  One pass
+ * over the state for all terms, FP64 accumulation. */
+int qgb_expect_pauli(const void* state, int nqubits, int dtype, const uint64_t* xmask,
+                     const uint64_t* zmask, const double* coef, int nterms, double* out,
+                     void* scratch, void* stream);
+size_t qgb_expect_scratch_bytes(int nqubits, int nterms);
+/* out (device) = Re sum_i conj(psi_i) (H psi)_i for a dense Hermitian H
+ * (device, complex128 interleaved, row-major 2^n x 2^n, n <= 20):
+ * Backend.expectation_value (backends/abstract.py:2807-2825) without the
+ * normalisation, which the caller applies with qgb_norm2.  ``scratch``:
+ * qgb_expect_scratch_bytes(nqubits, 1) bytes. */
+int qgb_expect_dense(const void* state, int nqubits, int dtype, const double* hamiltonian, double* out,
+                     void* scratch, void* stream);
+
+/* ---- timing helpers (events on the caller's stream) ------------------- */
+int qgb_event_create(void** ev);
+int qgb_event_destroy(void* ev);
+int qgb_event_record(void* ev, void* stream);
+int qgb_event_elapsed_ms(void* start, void* stop, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGB300_H */

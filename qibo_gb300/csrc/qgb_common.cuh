@@ -1,0 +1,128 @@
+// Shared types and helpers of the GB300 state-vector engine.
+//
+// Amplitude "traits" separate how an amplitude is stored in HBM from how it
+// is computed on:
+//   TC64   complex64: float2 in HBM, FP32 arithmetic.
+//   TC128  complex128: double2 in HBM, IEEE FP64 arithmetic.
+// Kernels are templates over a traits type, so every kernel exists for every
+// precision.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/qgb300.h"
+
+typedef int64_t i64;
+typedef uint64_t u64;
+
+#define QGB_MAXQ 40          // largest supported qubit count (index math is 64-bit)
+#define QGB_MAX_CTRL 8
+#define QGB_MAX_K 5          // largest dense gate (2^5 x 2^5)
+
+// ---------------------------------------------------------------- errors --
+void qgb_set_error(const char* fmt, ...);
+int qgb_cuda_status(cudaError_t e, const char* what);
+
+#define QGB_TRY_CUDA(call)                                   \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return qgb_cuda_status(_e, #call); \
+  } while (0)
+
+void qgb_count_launch();
+
+// after every kernel launch: count it and turn a launch error into a status
+#define QGB_LAUNCH_CHECK(what)                                       \
+  do {                                                               \
+    qgb_count_launch();                                              \
+    cudaError_t _e = cudaGetLastError();                             \
+    if (_e != cudaSuccess) return qgb_cuda_status(_e, what);         \
+  } while (0)
+
+int qgb_num_sms();
+
+// --------------------------------------------------------- complex math --
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// acc + a*b
+__host__ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 acc) {
+  return make_float2(fmaf(-a.y, b.y, fmaf(a.x, b.x, acc.x)), fmaf(a.y, b.x, fmaf(a.x, b.y, acc.y)));
+}
+__host__ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 acc) {
+  return make_double2(fma(-a.y, b.y, fma(a.x, b.x, acc.x)), fma(a.y, b.x, fma(a.x, b.y, acc.y)));
+}
+
+struct TC64 {
+  typedef float2 S;   // storage
+  typedef float2 V;   // value computed on
+  typedef float R;
+  static constexpr int kind = QGB_C64;
+  __host__ __device__ static V coef(double re, double im) { return make_float2((float)re, (float)im); }
+  __device__ static V zero() { return make_float2(0.f, 0.f); }
+  __device__ static V load(const S* p, i64 i) { return p[i]; }
+  __device__ static void store(S* p, i64 i, V v) { p[i] = v; }
+  __device__ static V mul(V a, V b) { return cmul(a, b); }
+  __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
+  __device__ static double abs2(V a) { return (double)a.x * a.x + (double)a.y * a.y; }
+  __device__ static V scale(V a, double s) { return make_float2((float)(a.x * s), (float)(a.y * s)); }
+  __device__ static V neg(V a) { return make_float2(-a.x, -a.y); }
+  __device__ static double re(V a) { return a.x; }
+  __device__ static double im(V a) { return a.y; }
+};
+
+struct TC128 {
+  typedef double2 S;
+  typedef double2 V;
+  typedef double R;
+  static constexpr int kind = QGB_C128;
+  __host__ __device__ static V coef(double re, double im) { return make_double2(re, im); }
+  __device__ static V zero() { return make_double2(0., 0.); }
+  __device__ static V load(const S* p, i64 i) { return p[i]; }
+  __device__ static void store(S* p, i64 i, V v) { p[i] = v; }
+  __device__ static V mul(V a, V b) { return cmul(a, b); }
+  __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
+  __device__ static double abs2(V a) { return fma_d(a.x, a.x, a.y * a.y); }
+  __device__ static double fma_d(double a, double b, double c) { return ::fma(a, b, c); }
+  __device__ static V scale(V a, double s) { return make_double2(a.x * s, a.y * s); }
+  __device__ static V neg(V a) { return make_double2(-a.x, -a.y); }
+  __device__ static double re(V a) { return a.x; }
+  __device__ static double im(V a) { return a.y; }
+};
+
+// ------------------------------------------------------- index helpers --
+// Positions are amplitude-index bit positions (bit b has stride 2^b).
+// qibo qubit q of an n-qubit state sits at bit n-1-q.
+struct BitInsert {
+  int n;          // number of inserted (fixed) bits
+  int pos[QGB_MAX_K + QGB_MAX_CTRL + 2];  // ascending
+};
+
+// Insert a zero at every position of ``bi`` (ascending order) into t.
+__device__ __forceinline__ i64 insert_zeros(i64 t, const BitInsert& bi) {
+#pragma unroll 4
+  for (int j = 0; j < bi.n; ++j) {
+    const int p = bi.pos[j];
+    t = ((t >> p) << (p + 1)) | (t & ((((i64)1) << p) - 1));
+  }
+  return t;
+}
+
+// Launch geometry: grid-stride loops with a grid that is a multiple of the
+// SM count (152 on GB300), capped so each thread does several items.
+inline void grid_for(i64 items, int threads, int* blocks) {
+  const int sms = qgb_num_sms();
+  i64 b = (items + threads - 1) / threads;
+  i64 cap = (i64)sms * 16;  // 16 resident-ish CTAs of 256 threads per SM
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  *blocks = (int)b;
+}
+
+inline int dtype_bytes(int dtype) { return dtype == QGB_C128 ? 16 : 8; }
+inline bool dtype_ok(int dtype) { return dtype == QGB_C64 || dtype == QGB_C128; }

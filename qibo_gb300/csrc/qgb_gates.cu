@@ -1,0 +1,494 @@
+// Gate application: the GB300 replacement of Backend.apply_gate
+// (backends/abstract.py:2322-2361) and Backend._apply_gate_controlled_by
+// (backends/abstract.py:3176-3197).
+//
+// The reference moves the gate's qubit axes to the front with a transpose
+// (a full copy), multiplies by the 2^k x 2^k matrix and transposes back.
+// Here every gate is one in-place pass over only the amplitudes it changes:
+//   * dense k-qubit gates gather the 2^k amplitudes of a group, multiply
+//     and scatter back (k = 1 with a warp-shuffle variant for low bits);
+//   * diagonal gates whose only non-unit entry sits on the all-ones corner
+//     (CZ, CU1, CCZ, S, T, Z, U1 and controlled versions) multiply a phase
+//     into 2^(n-c) amplitudes only;
+//   * other diagonal gates (RZ, RZZ, CRZ) scale in place;
+//   * X-like gates (X, Y, CNOT, CY, TOFFOLI) and SWAP move data only.
+// The host-side classifier (``qgb_apply_gate``) finds "hidden" controls in
+// a matrix (an axis on which the matrix is the identity when that qubit is
+// 0), so CU1 / CNOT / TOFFOLI / CZ given as full matrices take the cheap
+// kernels.
+#include <algorithm>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "qgb_common.cuh"
+
+typedef std::complex<double> zd;
+
+template <int K>
+struct Offs { i64 o[1 << K]; };
+
+template <typename T, int K>
+struct DenseMat { typename T::V m[1 << K][1 << K]; };
+
+// ---------------------------------------------------------------------------
+// dense k-qubit gate with optional controls (generic)
+template <typename T, int K>
+__global__ void __launch_bounds__(256) k_dense(typename T::S* __restrict__ psi, i64 ngroups, BitInsert bi,
+                                               i64 cmask, Offs<K> off, DenseMat<T, K> M) {
+  constexpr int D = 1 << K;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < ngroups; t += stride) {
+    const i64 base = insert_zeros(t, bi) | cmask;
+    typename T::V v[D];
+#pragma unroll
+    for (int m = 0; m < D; ++m) v[m] = T::load(psi, base + off.o[m]);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      typename T::V acc = T::mul(M.m[r][0], v[0]);
+#pragma unroll
+      for (int c = 1; c < D; ++c) acc = T::fma(M.m[r][c], v[c], acc);
+      T::store(psi, base + off.o[r], acc);
+    }
+  }
+}
+
+// dense 1-qubit gate, no controls, target bit >= 5: independent pairs,
+// coalesced 16-byte (c128) / 8-byte (c64) accesses, two pairs per thread.
+template <typename T>
+__global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ psi, i64 npairs, int b,
+                                                  typename T::V u00, typename T::V u01,
+                                                  typename T::V u10, typename T::V u11) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  const i64 lowmask = ((i64)1 << b) - 1;
+  const i64 step = (i64)1 << b;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < npairs; t += 2 * stride) {
+    const i64 t2 = t + stride;
+    const i64 i0 = ((t >> b) << (b + 1)) | (t & lowmask);
+    const bool has2 = t2 < npairs;
+    const i64 j0 = ((t2 >> b) << (b + 1)) | (t2 & lowmask);
+    typename T::V a0 = T::load(psi, i0), a1 = T::load(psi, i0 + step);
+    typename T::V c0, c1;
+    if (has2) { c0 = T::load(psi, j0); c1 = T::load(psi, j0 + step); }
+    T::store(psi, i0, T::fma(u01, a1, T::mul(u00, a0)));
+    T::store(psi, i0 + step, T::fma(u11, a1, T::mul(u10, a0)));
+    if (has2) {
+      T::store(psi, j0, T::fma(u01, c1, T::mul(u00, c0)));
+      T::store(psi, j0 + step, T::fma(u11, c1, T::mul(u10, c0)));
+    }
+  }
+}
+
+template <typename V>
+__device__ __forceinline__ V shfl_xor_v(V v, int mask);
+template <>
+__device__ __forceinline__ float2 shfl_xor_v(float2 v, int mask) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
+}
+template <>
+__device__ __forceinline__ double2 shfl_xor_v(double2 v, int mask) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
+}
+
+// dense 1-qubit gate, no controls, target bit < 5: each lane owns one
+// amplitude of a contiguous 32-amplitude window and fetches its partner
+// (lane ^ 2^b) with a warp shuffle.  Requires N >= 32 and a whole number of
+// warps per window (the grid covers N exactly in warps).
+template <typename T>
+__global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi, i64 N, int b,
+                                                 typename T::V u00, typename T::V u01,
+                                                 typename T::V u10, typename T::V u11) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const bool hi = (lane >> b) & 1;
+  const typename T::V cs = hi ? u11 : u00;  // coefficient of own amplitude
+  const typename T::V cp = hi ? u10 : u01;  // coefficient of the partner
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
+    // N is a multiple of 32 and stride is a multiple of 32: whole warps stay
+    // in the loop together, so the full-mask shuffle is safe.
+    typename T::V a = T::load(psi, i);
+    typename T::V p = shfl_xor_v(a, 1 << b);
+    T::store(psi, i, T::fma(cp, p, T::mul(cs, a)));
+  }
+}
+
+// multiply ``phase`` into every amplitude whose ``mask`` bits are all 1
+template <typename T>
+__global__ void __launch_bounds__(256) k_phase(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+                                               i64 mask, typename T::V phase) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const i64 i = insert_zeros(t, bi) | mask;
+    T::store(psi, i, T::mul(phase, T::load(psi, i)));
+  }
+}
+
+// diagonal k-qubit gate with controls: amplitude *= d[target bits]
+template <typename T>
+struct DiagVec { typename T::V d[32]; };
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_diagk(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+                                               i64 cmask, int k, Offs<QGB_MAX_K> tbit, DiagVec<T> D) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const i64 i = insert_zeros(t, bi) | cmask;
+    int m = 0;
+    for (int j = 0; j < k; ++j) m = (m << 1) | (int)((i >> tbit.o[j]) & 1);
+    T::store(psi, i, T::mul(D.d[m], T::load(psi, i)));
+  }
+}
+
+// X-like 1-qubit gate [[0, a], [b, 0]] with controls: new0 = a*old1, new1 = b*old0
+template <typename T>
+__global__ void __launch_bounds__(256) k_xlike(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+                                               i64 cmask, i64 tstep, typename T::V a, typename T::V b,
+                                               int plain) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const i64 i0 = insert_zeros(t, bi) | cmask;
+    typename T::V v0 = T::load(psi, i0), v1 = T::load(psi, i0 + tstep);
+    if (plain) {
+      T::store(psi, i0, v1);
+      T::store(psi, i0 + tstep, v0);
+    } else {
+      T::store(psi, i0, T::mul(a, v1));
+      T::store(psi, i0 + tstep, T::mul(b, v0));
+    }
+  }
+}
+
+// SWAP of bits (a, b) with controls: exchanges |..0..1..> and |..1..0..>
+template <typename T>
+__global__ void __launch_bounds__(256) k_swap(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+                                              i64 cmask, i64 sa, i64 sb) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const i64 base = insert_zeros(t, bi) | cmask;
+    typename T::V v01 = T::load(psi, base | sb), v10 = T::load(psi, base | sa);
+    T::store(psi, base | sb, v10);
+    T::store(psi, base | sa, v01);
+  }
+}
+
+// ===========================================================================
+// host side
+namespace {
+
+struct Geometry {
+  int n;
+  std::vector<int> tbits;   // target bit positions, matrix order
+  std::vector<int> cbits;   // control bit positions
+};
+
+int validate(void* state, int n, int dtype, const int* qubits, int k, const int* controls, int nc,
+             const char* fn, Geometry* g) {
+  if (!state) { qgb_set_error("%s: null state", fn); return QGB_ERR_INVALID; }
+  if (n < 1 || n > QGB_MAXQ) { qgb_set_error("%s: nqubits=%d out of range", fn, n); return QGB_ERR_INVALID; }
+  if (!dtype_ok(dtype)) { qgb_set_error("%s: unknown dtype %d", fn, dtype); return QGB_ERR_INVALID; }
+  if (k < 0 || k > QGB_MAX_K) { qgb_set_error("%s: %d target qubits (max %d)", fn, k, QGB_MAX_K); return QGB_ERR_UNSUPPORTED; }
+  if (nc < 0 || nc > QGB_MAX_CTRL) { qgb_set_error("%s: %d controls (max %d)", fn, nc, QGB_MAX_CTRL); return QGB_ERR_UNSUPPORTED; }
+  u64 seen = 0;
+  g->n = n;
+  g->tbits.clear();
+  g->cbits.clear();
+  for (int j = 0; j < k + nc; ++j) {
+    int q = j < k ? qubits[j] : controls[j - k];
+    if (q < 0 || q >= n) { qgb_set_error("%s: qubit %d out of range for %d qubits", fn, q, n); return QGB_ERR_INVALID; }
+    if (seen & (1ull << q)) { qgb_set_error("%s: qubit %d repeated", fn, q); return QGB_ERR_INVALID; }
+    seen |= 1ull << q;
+    (j < k ? g->tbits : g->cbits).push_back(n - 1 - q);
+  }
+  return QGB_OK;
+}
+
+BitInsert make_insert(std::vector<int> bits) {
+  BitInsert bi;
+  std::sort(bits.begin(), bits.end());
+  bi.n = (int)bits.size();
+  for (int j = 0; j < bi.n; ++j) bi.pos[j] = bits[j];
+  return bi;
+}
+
+i64 mask_of(const std::vector<int>& bits) {
+  i64 m = 0;
+  for (int b : bits) m |= (i64)1 << b;
+  return m;
+}
+
+template <typename T>
+int launch_dense(void* state, const Geometry& g, const std::vector<zd>& M, cudaStream_t s) {
+  const int k = (int)g.tbits.size();
+  std::vector<int> fixed = g.tbits;
+  fixed.insert(fixed.end(), g.cbits.begin(), g.cbits.end());
+  BitInsert bi = make_insert(fixed);
+  const i64 cmask = mask_of(g.cbits);
+  const i64 ngroups = (i64)1 << (g.n - (int)fixed.size());
+  const int D = 1 << k;
+  typedef typename T::S S;
+  // fast 1-qubit paths (no controls)
+  if (k == 1 && g.cbits.empty()) {
+    const int b = g.tbits[0];
+    typename T::V u00 = T::coef(M[0].real(), M[0].imag()), u01 = T::coef(M[1].real(), M[1].imag());
+    typename T::V u10 = T::coef(M[2].real(), M[2].imag()), u11 = T::coef(M[3].real(), M[3].imag());
+    if (b < 5 && g.n >= 5) {
+      const i64 N = (i64)1 << g.n;
+      int blocks;
+      grid_for(N, 256, &blocks);
+      k_1q_shfl<T><<<blocks, 256, 0, s>>>((S*)state, N, b, u00, u01, u10, u11);
+      QGB_LAUNCH_CHECK("k_1q_shfl");
+      return QGB_OK;
+    }
+    if (b >= 5) {
+      int blocks;
+      grid_for((ngroups + 1) / 2, 256, &blocks);
+      k_1q_pairs<T><<<blocks, 256, 0, s>>>((S*)state, ngroups, b, u00, u01, u10, u11);
+      QGB_LAUNCH_CHECK("k_1q_pairs");
+      return QGB_OK;
+    }
+  }
+  int blocks;
+  grid_for(ngroups, 256, &blocks);
+#define QGB_DENSE_CASE(KK)                                                              \
+  case KK: {                                                                            \
+    Offs<KK> off;                                                                       \
+    DenseMat<T, KK> dm;                                                                 \
+    for (int m = 0; m < D; ++m) {                                                       \
+      i64 o = 0;                                                                        \
+      for (int j = 0; j < k; ++j)                                                       \
+        if ((m >> (k - 1 - j)) & 1) o |= (i64)1 << g.tbits[j];                          \
+      off.o[m] = o;                                                                     \
+    }                                                                                   \
+    for (int r = 0; r < D; ++r)                                                         \
+      for (int c = 0; c < D; ++c) dm.m[r][c] = T::coef(M[r * D + c].real(), M[r * D + c].imag()); \
+    k_dense<T, KK><<<blocks, 256, 0, s>>>((S*)state, ngroups, bi, cmask, off, dm);      \
+    QGB_LAUNCH_CHECK("k_dense");                                                        \
+    return QGB_OK;                                                                      \
+  }
+  switch (k) {
+    QGB_DENSE_CASE(1)
+    QGB_DENSE_CASE(2)
+    QGB_DENSE_CASE(3)
+    QGB_DENSE_CASE(4)
+    QGB_DENSE_CASE(5)
+    default:
+      qgb_set_error("dense gate with %d qubits unsupported", k);
+      return QGB_ERR_UNSUPPORTED;
+  }
+#undef QGB_DENSE_CASE
+}
+
+template <typename T>
+int launch_phase(void* state, int n, const std::vector<int>& bits, zd ph, cudaStream_t s) {
+  if (ph == zd(1.0, 0.0)) return QGB_OK;
+  BitInsert bi = make_insert(bits);
+  const i64 count = (i64)1 << (n - (int)bits.size());
+  int blocks;
+  grid_for(count, 256, &blocks);
+  k_phase<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(bits), T::coef(ph.real(), ph.imag()));
+  QGB_LAUNCH_CHECK("k_phase");
+  return QGB_OK;
+}
+
+template <typename T>
+int launch_diag(void* state, const Geometry& g, const std::vector<zd>& d, cudaStream_t s) {
+  const int k = (int)g.tbits.size();
+  BitInsert bi = make_insert(g.cbits);
+  const i64 count = (i64)1 << (g.n - (int)g.cbits.size());
+  Offs<QGB_MAX_K> tb;
+  for (int j = 0; j < QGB_MAX_K; ++j) tb.o[j] = j < k ? g.tbits[j] : 0;
+  DiagVec<T> D;
+  for (int m = 0; m < 32; ++m) D.d[m] = m < (1 << k) ? T::coef(d[m].real(), d[m].imag()) : T::coef(1.0, 0.0);
+  int blocks;
+  grid_for(count, 256, &blocks);
+  k_diagk<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), k, tb, D);
+  QGB_LAUNCH_CHECK("k_diagk");
+  return QGB_OK;
+}
+
+template <typename T>
+int launch_xlike(void* state, const Geometry& g, zd a, zd b, cudaStream_t s) {
+  std::vector<int> fixed = g.cbits;
+  fixed.push_back(g.tbits[0]);
+  BitInsert bi = make_insert(fixed);
+  const i64 count = (i64)1 << (g.n - (int)fixed.size());
+  int blocks;
+  grid_for(count, 256, &blocks);
+  const int plain = (a == zd(1, 0) && b == zd(1, 0)) ? 1 : 0;
+  k_xlike<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), (i64)1 << g.tbits[0],
+                                    T::coef(a.real(), a.imag()), T::coef(b.real(), b.imag()), plain);
+  QGB_LAUNCH_CHECK("k_xlike");
+  return QGB_OK;
+}
+
+template <typename T>
+int launch_swap(void* state, const Geometry& g, cudaStream_t s) {
+  std::vector<int> fixed = g.cbits;
+  fixed.push_back(g.tbits[0]);
+  fixed.push_back(g.tbits[1]);
+  BitInsert bi = make_insert(fixed);
+  const i64 count = (i64)1 << (g.n - (int)fixed.size());
+  int blocks;
+  grid_for(count, 256, &blocks);
+  k_swap<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), (i64)1 << g.tbits[0],
+                                   (i64)1 << g.tbits[1]);
+  QGB_LAUNCH_CHECK("k_swap");
+  return QGB_OK;
+}
+
+// Move target j of (g, M) into the controls when the matrix is the identity
+// on the subspace where that qubit is 0 and does not couple it to the 1
+// subspace.  Returns true when a control was extracted.
+bool extract_control(Geometry& g, std::vector<zd>& M) {
+  const int k = (int)g.tbits.size();
+  const int D = 1 << k;
+  for (int j = 0; j < k; ++j) {
+    const int bit = 1 << (k - 1 - j);
+    bool ok = true;
+    for (int r = 0; r < D && ok; ++r)
+      for (int c = 0; c < D && ok; ++c) {
+        if ((r & bit) && (c & bit)) continue;
+        const zd want = (r == c) ? zd(1, 0) : zd(0, 0);
+        if (M[r * D + c] != want) ok = false;
+      }
+    if (!ok) continue;
+    // keep rows/cols with the bit set
+    std::vector<zd> R((D / 2) * (D / 2));
+    int ri = 0;
+    for (int r = 0; r < D; ++r) {
+      if (!(r & bit)) continue;
+      int ci = 0;
+      for (int c = 0; c < D; ++c) {
+        if (!(c & bit)) continue;
+        R[ri * (D / 2) + ci] = M[r * D + c];
+        ++ci;
+      }
+      ++ri;
+    }
+    g.cbits.push_back(g.tbits[j]);
+    g.tbits.erase(g.tbits.begin() + j);
+    M.swap(R);
+    return true;
+  }
+  return false;
+}
+
+template <typename T>
+int dispatch(void* state, Geometry g, std::vector<zd> M, cudaStream_t s) {
+  while (!g.tbits.empty() && extract_control(g, M)) {
+  }
+  const int k = (int)g.tbits.size();
+  const int D = 1 << k;
+  if (k == 0) return launch_phase<T>(state, g.n, g.cbits, M[0], s);
+  bool diag = true, offdiag1 = (k == 1);
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) {
+      if (r != c && M[r * D + c] != zd(0, 0)) diag = false;
+      if (k == 1 && r == c && M[r * D + c] != zd(0, 0)) offdiag1 = false;
+    }
+  if (diag) {
+    // diag(1, ..., 1, phase) with a single target was caught as a control;
+    // a diagonal with a unit first entry on one target is a phase on its 1s
+    if (k == 1 && M[0] == zd(1, 0)) {
+      std::vector<int> bits = g.cbits;
+      bits.push_back(g.tbits[0]);
+      return launch_phase<T>(state, g.n, bits, M[3], s);
+    }
+    std::vector<zd> d(D);
+    for (int m = 0; m < D; ++m) d[m] = M[m * D + m];
+    return launch_diag<T>(state, g, d, s);
+  }
+  if (offdiag1) return launch_xlike<T>(state, g, M[1], M[2], s);
+  if (k == 2) {
+    const zd one(1, 0), zero(0, 0);
+    const zd sw[16] = {one, zero, zero, zero, zero, zero, one, zero, zero, one, zero, zero, zero, zero, zero, one};
+    bool is_swap = true;
+    for (int i = 0; i < 16; ++i)
+      if (M[i] != sw[i]) is_swap = false;
+    if (is_swap) return launch_swap<T>(state, g, s);
+  }
+  return launch_dense<T>(state, g, M, s);
+}
+
+std::vector<zd> read_matrix(const double* m, int k) {
+  const int D = 1 << k;
+  std::vector<zd> M(D * D);
+  for (int i = 0; i < D * D; ++i) M[i] = zd(m[2 * i], m[2 * i + 1]);
+  return M;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qgb_apply_gate(void* state, int nqubits, int dtype, const int* qubits, int k, const int* controls,
+                   int ncontrols, const double* matrix, void* stream) {
+  Geometry g;
+  int st = validate(state, nqubits, dtype, qubits, k, controls, ncontrols, "qgb_apply_gate", &g);
+  if (st) return st;
+  if (!matrix) { qgb_set_error("qgb_apply_gate: null matrix"); return QGB_ERR_INVALID; }
+  std::vector<zd> M = read_matrix(matrix, k);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? dispatch<TC128>(state, g, M, s) : dispatch<TC64>(state, g, M, s);
+}
+
+int qgb_apply_1q(void* state, int nqubits, int dtype, int target, const double* matrix, void* stream) {
+  Geometry g;
+  int st = validate(state, nqubits, dtype, &target, 1, nullptr, 0, "qgb_apply_1q", &g);
+  if (st) return st;
+  std::vector<zd> M = read_matrix(matrix, 1);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? launch_dense<TC128>(state, g, M, s) : launch_dense<TC64>(state, g, M, s);
+}
+
+int qgb_apply_2q(void* state, int nqubits, int dtype, int q0, int q1, const double* matrix, void* stream) {
+  Geometry g;
+  int qs[2] = {q0, q1};
+  int st = validate(state, nqubits, dtype, qs, 2, nullptr, 0, "qgb_apply_2q", &g);
+  if (st) return st;
+  std::vector<zd> M = read_matrix(matrix, 2);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? launch_dense<TC128>(state, g, M, s) : launch_dense<TC64>(state, g, M, s);
+}
+
+int qgb_apply_phase(void* state, int nqubits, int dtype, const int* qubits, int nq, double phase_re,
+                    double phase_im, void* stream) {
+  Geometry g;
+  int st = validate(state, nqubits, dtype, nullptr, 0, qubits, nq, "qgb_apply_phase", &g);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  zd ph(phase_re, phase_im);
+  return dtype == QGB_C128 ? launch_phase<TC128>(state, nqubits, g.cbits, ph, s)
+                           : launch_phase<TC64>(state, nqubits, g.cbits, ph, s);
+}
+
+int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1, const int* controls, int ncontrols,
+                   void* stream) {
+  Geometry g;
+  int qs[2] = {q0, q1};
+  int st = validate(state, nqubits, dtype, qs, 2, controls, ncontrols, "qgb_apply_swap", &g);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? launch_swap<TC128>(state, g, s) : launch_swap<TC64>(state, g, s);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// whole circuits
+int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
+                    cudaStream_t s);  // qgb_blocked.cu
+
+extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
+                                 const double* coefs, int flags, void* stream) {
+  if (nops < 0 || (nops > 0 && (!ops || !coefs))) { qgb_set_error("qgb_apply_circuit: bad arguments"); return QGB_ERR_INVALID; }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (flags & QGB_PLAN_BLOCKED) return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, s);
+  for (int i = 0; i < nops; ++i) {
+    const qgb_op& op = ops[i];
+    int st = qgb_apply_gate(state, nqubits, dtype, op.qubits, op.k, op.controls, op.ncontrols,
+                            coefs + op.coef_offset, stream);
+    if (st) return st;
+  }
+  return QGB_OK;
+}

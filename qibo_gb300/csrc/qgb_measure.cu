@@ -1,0 +1,680 @@
+// Measurement and observables on the device:
+//  * marginal probabilities (Backend.calculate_probabilities,
+//    backends/abstract.py:2734-2758, ordered as _order_probabilities
+//    :3371-3381) with FP64 accumulation and a deterministic two-stage
+//    reduction (no floating-point atomics: the same input gives the same
+//    bits on every run);
+//  * the squared norm;
+//  * shot sampling (Backend.sample_shots / sample_frequencies,
+//    :2760-2801): an FP64 two-level CDF (inclusive prefix over 64-entry
+//    chunk sums, then an in-chunk running sum) searched by one thread per
+//    shot with uniforms from a Philox4x32-10 counter-based stream (Salmon,
+//    Moraes, Dror, Shaw, SC'11), so each shot's draw depends only on
+//    (seed, shot index);
+//  * Pauli-sum expectation values (Backend.exp_value_observable_symbolic,
+//    :2946-3054): one pass per distinct X/Y flip mask covering all terms
+//    that share it, instead of one einsum pass per term.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "qgb_common.cuh"
+
+// ------------------------------------------------------------ reductions --
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// deterministic block sum (256 threads): result valid in thread 0
+__device__ double block_sum256(double v) {
+  __shared__ double sh[8];
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (l < 8) ? sh[l] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+__host__ __device__ __forceinline__ i64 imin64(i64 a, i64 b) { return a < b ? a : b; }
+
+// insert a zero at each of the ascending positions pos[0..n)
+__device__ __forceinline__ i64 insert_zeros_n(i64 t, const int* pos, int n) {
+  for (int j = 0; j < n; ++j) {
+    const int p = pos[j];
+    t = ((t >> p) << (p + 1)) | (t & ((((i64)1) << p) - 1));
+  }
+  return t;
+}
+
+// deposit the low bits of v into the (ascending) positions pos[0..n)
+__device__ __forceinline__ i64 deposit(i64 v, const int* pos, int n) {
+  i64 r = 0;
+  for (int j = 0; j < n; ++j) r |= ((v >> j) & 1) << pos[j];
+  return r;
+}
+
+struct ProbGeom {
+  int n, nq, u;
+  int mpos[QGB_MAXQ];  // measured bit positions, output-bit order: mpos[j] <-> output bit j
+  int msorted[QGB_MAXQ];  // measured positions ascending
+  int upos[QGB_MAXQ];  // unmeasured positions ascending
+};
+
+// all qubits measured: out[j] = |psi[i]|^2 with j = gathered bits of i
+template <typename T>
+__global__ void __launch_bounds__(256) k_probs_all(const typename T::S* __restrict__ psi, i64 N, ProbGeom g,
+                                                   int identity, double* __restrict__ out) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double p = T::abs2(T::load(psi, i));
+    i64 j = i;
+    if (!identity) {
+      j = 0;
+      for (int b = 0; b < g.nq; ++b) j |= ((i >> g.mpos[b]) & 1) << b;
+    }
+    out[j] = p;
+  }
+}
+
+// few unmeasured qubits: one thread per output sums its 2^u amplitudes
+template <typename T>
+__global__ void __launch_bounds__(256) k_probs_thread(const typename T::S* __restrict__ psi, i64 nout, ProbGeom g,
+                                                      double* __restrict__ out) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  const i64 nr = (i64)1 << g.u;
+  for (i64 j = blockIdx.x * (i64)blockDim.x + threadIdx.x; j < nout; j += stride) {
+    i64 base = 0;
+    for (int b = 0; b < g.nq; ++b) base |= ((j >> b) & 1) << g.mpos[b];
+    double acc = 0.0;
+    for (i64 r = 0; r < nr; ++r) acc += T::abs2(T::load(psi, base | deposit(r, g.upos, g.u)));
+    out[j] = acc;
+  }
+}
+
+// many unmeasured qubits: block (j, p) sums part p of output j's amplitudes
+template <typename T>
+__global__ void __launch_bounds__(256) k_probs_block(const typename T::S* __restrict__ psi, int parts, i64 per_part,
+                                                     ProbGeom g, double* __restrict__ dst) {
+  const i64 j = blockIdx.x / parts;
+  const int p = blockIdx.x % parts;
+  i64 base = 0;
+  for (int b = 0; b < g.nq; ++b) base |= ((j >> b) & 1) << g.mpos[b];
+  double acc = 0.0;
+  const i64 r0 = (i64)p * per_part;
+  for (i64 r = r0 + threadIdx.x; r < r0 + per_part; r += blockDim.x) {
+    // unmeasured index r -> amplitude index: insert zeros at measured positions
+    const i64 idx = insert_zeros_n(r, g.msorted, g.nq) | base;
+    acc += T::abs2(T::load(psi, idx));
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) dst[blockIdx.x] = acc;
+}
+
+// out[j] = sum_p src[j*parts + p], one warp per output, fixed order
+__global__ void k_sum_parts(const double* __restrict__ src, i64 nout, int parts, double* __restrict__ out) {
+  const i64 warp = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nout) return;
+  double acc = 0.0;
+  for (int p = lane; p < parts; p += 32) acc += src[warp * parts + p];
+  acc = warp_sum(acc);
+  if (lane == 0) out[warp] = acc;
+}
+
+namespace {
+
+int prob_plan(int n, int nq, i64* parts, i64* per_part) {
+  const int u = n - nq;
+  if (u <= 10) { *parts = 0; *per_part = 0; return 0; }
+  const i64 items = (i64)1 << u;
+  i64 pp = std::max<i64>(8192, items / 1024);
+  *per_part = pp;
+  *parts = items / pp;
+  return 0;
+}
+
+template <typename T>
+int probs_impl(const void* state, int n, const int* qubits, int nq, double* out, void* scratch, cudaStream_t s) {
+  ProbGeom g;
+  g.n = n;
+  g.nq = nq;
+  g.u = n - nq;
+  std::vector<int> mbits;
+  u64 seen = 0;
+  for (int j = 0; j < nq; ++j) {
+    const int q = qubits[j];
+    if (q < 0 || q >= n) { qgb_set_error("qgb_probabilities: qubit %d out of range", q); return QGB_ERR_INVALID; }
+    if (seen & (1ull << q)) { qgb_set_error("qgb_probabilities: qubit %d repeated", q); return QGB_ERR_INVALID; }
+    seen |= 1ull << q;
+    // qubits[0] is the most significant output bit
+    g.mpos[nq - 1 - j] = n - 1 - q;
+    mbits.push_back(n - 1 - q);
+  }
+  int ui = 0;
+  for (int b = 0; b < n; ++b)
+    if (std::find(mbits.begin(), mbits.end(), b) == mbits.end()) g.upos[ui++] = b;
+  std::vector<int> sorted = mbits;
+  std::sort(sorted.begin(), sorted.end());
+  for (int j = 0; j < nq; ++j) g.msorted[j] = sorted[j];
+  typedef typename T::S S;
+  const i64 nout = (i64)1 << nq;
+  if (g.u == 0) {
+    bool identity = true;
+    for (int b = 0; b < nq; ++b)
+      if (g.mpos[b] != b) identity = false;
+    int blocks;
+    grid_for(nout, 256, &blocks);
+    k_probs_all<T><<<blocks, 256, 0, s>>>((const S*)state, nout, g, identity ? 1 : 0, out);
+    QGB_LAUNCH_CHECK("k_probs_all");
+    return QGB_OK;
+  }
+  i64 parts, per_part;
+  prob_plan(n, nq, &parts, &per_part);
+  if (parts == 0) {
+    int blocks;
+    grid_for(nout, 256, &blocks);
+    k_probs_thread<T><<<blocks, 256, 0, s>>>((const S*)state, nout, g, out);
+    QGB_LAUNCH_CHECK("k_probs_thread");
+    return QGB_OK;
+  }
+  const i64 nblocks = nout * parts;
+  if (parts == 1) {
+    k_probs_block<T><<<(unsigned)nblocks, 256, 0, s>>>((const S*)state, 1, per_part, g, out);
+    QGB_LAUNCH_CHECK("k_probs_block");
+    return QGB_OK;
+  }
+  if (!scratch) { qgb_set_error("qgb_probabilities: scratch buffer required"); return QGB_ERR_INVALID; }
+  double* part = (double*)scratch;
+  k_probs_block<T><<<(unsigned)nblocks, 256, 0, s>>>((const S*)state, (int)parts, per_part, g, part);
+  QGB_LAUNCH_CHECK("k_probs_block");
+  const i64 threads = nout * 32;
+  k_sum_parts<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(part, nout, (int)parts, out);
+  QGB_LAUNCH_CHECK("k_sum_parts");
+  return QGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t qgb_probs_scratch_bytes(int nqubits, int nq) {
+  if (nq < 0 || nq > nqubits) return 0;
+  i64 parts, per_part;
+  prob_plan(nqubits, nq, &parts, &per_part);
+  if (parts <= 1) return 0;
+  return (size_t)(((i64)1 << nq) * parts * sizeof(double));
+}
+
+int qgb_probabilities(const void* state, int nqubits, int dtype, const int* qubits, int nq, double* out,
+                      void* scratch, void* stream) {
+  if (!state || !out) { qgb_set_error("qgb_probabilities: null pointer"); return QGB_ERR_INVALID; }
+  if (nqubits < 1 || nqubits > QGB_MAXQ || nq < 0 || nq > nqubits) {
+    qgb_set_error("qgb_probabilities: bad sizes n=%d nq=%d", nqubits, nq);
+    return QGB_ERR_INVALID;
+  }
+  if (!dtype_ok(dtype)) { qgb_set_error("qgb_probabilities: bad dtype"); return QGB_ERR_INVALID; }
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? probs_impl<TC128>(state, nqubits, qubits, nq, out, scratch, s)
+                           : probs_impl<TC64>(state, nqubits, qubits, nq, out, scratch, s);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ norm --
+template <typename T>
+__global__ void __launch_bounds__(256) k_norm_part(const typename T::S* __restrict__ psi, i64 N,
+                                                   double* __restrict__ part) {
+  double acc = 0.0;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) acc += T::abs2(T::load(psi, i));
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void k_final_sum(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  double acc = 0.0;
+  for (int p = threadIdx.x; p < nparts; p += blockDim.x) acc += part[p];
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) *out = acc;
+}
+
+static const int kNormBlocksCap = 16 * 160;
+
+extern "C" size_t qgb_norm_scratch_bytes(void) { return (size_t)kNormBlocksCap * sizeof(double); }
+
+extern "C" int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scratch, void* stream) {
+  if (!state || !out || !scratch || nqubits < 1 || nqubits > QGB_MAXQ || !dtype_ok(dtype)) {
+    qgb_set_error("qgb_norm2: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  const i64 N = (i64)1 << nqubits;
+  int blocks;
+  grid_for(N, 256, &blocks);
+  if (blocks > kNormBlocksCap) blocks = kNormBlocksCap;
+  double* part = (double*)scratch;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == QGB_C128) k_norm_part<TC128><<<blocks, 256, 0, s>>>((const double2*)state, N, part);
+  else k_norm_part<TC64><<<blocks, 256, 0, s>>>((const float2*)state, N, part);
+  QGB_LAUNCH_CHECK("k_norm_part");
+  k_final_sum<<<1, 256, 0, s>>>(part, blocks, out);
+  QGB_LAUNCH_CHECK("k_final_sum");
+  return QGB_OK;
+}
+
+// -------------------------------------------------------------- sampling --
+// Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64
+// multiplications with the published multipliers and Weyl key increments.
+struct Philox4 { uint32_t v[4]; };
+
+__host__ __device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                          uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += W0; k1 += W1; }
+    const uint64_t p0 = (uint64_t)M0 * c0, p1 = (uint64_t)M1 * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  Philox4 r;
+  r.v[0] = c0; r.v[1] = c1; r.v[2] = c2; r.v[3] = c3;
+  return r;
+}
+
+// uniform double in [0, 1) with 53 random bits
+__device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) {
+  const uint64_t x = (((uint64_t)a << 32) | b) >> 11;
+  return (double)x * (1.0 / 9007199254740992.0);
+}
+
+#define QGB_CHUNK 64
+
+// chunk[c] = sequential sum of probs[c*64 .. c*64+64)
+__global__ void k_chunk_sums(const double* __restrict__ probs, i64 nprobs, i64 nchunks, double* __restrict__ chunk) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 c = blockIdx.x * (i64)blockDim.x + threadIdx.x; c < nchunks; c += stride) {
+    double acc = 0.0;
+    const i64 e = imin64(nprobs, (c + 1) * QGB_CHUNK);
+    for (i64 i = c * QGB_CHUNK; i < e; ++i) acc += probs[i];
+    chunk[c] = acc;
+  }
+}
+
+// in-place inclusive scan of 1024-element tiles (256 threads x 4); tile totals to tot
+__global__ void k_scan_tiles(double* __restrict__ a, i64 n, double* __restrict__ tot) {
+  __shared__ double sh[256];
+  const i64 base = (i64)blockIdx.x * 1024 + threadIdx.x * 4;
+  double v[4];
+  double run = 0.0;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    v[e] = (base + e < n) ? a[base + e] : 0.0;
+    run += v[e];
+    v[e] = run;
+  }
+  sh[threadIdx.x] = run;
+  __syncthreads();
+  // Hillis-Steele over the 256 thread totals
+  for (int off = 1; off < 256; off <<= 1) {
+    double add = (threadIdx.x >= off) ? sh[threadIdx.x - off] : 0.0;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  const double prefix = threadIdx.x > 0 ? sh[threadIdx.x - 1] : 0.0;
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (base + e < n) a[base + e] = v[e] + prefix;
+  if (threadIdx.x == 255 && tot) tot[blockIdx.x] = sh[255];
+}
+
+// add the exclusive prefix of tile totals (already scanned inclusively) to tiles 1..
+__global__ void k_scan_add(double* __restrict__ a, i64 n, const double* __restrict__ tot_scanned) {
+  const i64 t = blockIdx.x;
+  if (t == 0) return;
+  const double off = tot_scanned[t - 1];
+  for (i64 i = t * 1024 + threadIdx.x; i < imin64(n, (t + 1) * 1024); i += blockDim.x) a[i] += off;
+}
+
+template <bool COUNTS>
+__global__ void __launch_bounds__(256) k_draw(const double* __restrict__ probs, i64 nprobs,
+                                              const double* __restrict__ cdf, i64 nchunks, i64 nshots,
+                                              uint32_t k0, uint32_t k1, int64_t* __restrict__ dst) {
+  const double total = cdf[nchunks - 1];
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 s = blockIdx.x * (i64)blockDim.x + threadIdx.x; s < nshots; s += stride) {
+    Philox4 r = philox4x32_10((uint32_t)s, (uint32_t)(s >> 32), 0u, 0u, k0, k1);
+    const double target = u01_53(r.v[0], r.v[1]) * total;
+    // first chunk whose inclusive prefix exceeds target
+    i64 lo = 0, hi = nchunks - 1;
+    while (lo < hi) {
+      const i64 mid = (lo + hi) >> 1;
+      if (cdf[mid] > target) hi = mid; else lo = mid + 1;
+    }
+    double run = lo > 0 ? cdf[lo - 1] : 0.0;
+    const i64 b = lo * QGB_CHUNK, e = imin64(nprobs, b + QGB_CHUNK);
+    i64 pick = -1, last_nz = -1;
+    for (i64 i = b; i < e; ++i) {
+      const double p = probs[i];
+      if (p > 0.0) {
+        last_nz = i;
+        run += p;
+        if (run > target) { pick = i; break; }
+      }
+    }
+    if (pick < 0) pick = last_nz;  // rounding between the two CDF levels
+    if (pick < 0) pick = b;        // all-zero distribution: caller error, stay in bounds
+    if (COUNTS) atomicAdd((unsigned long long*)&dst[pick], 1ull);
+    else dst[s] = pick;
+  }
+}
+
+__global__ void k_philox_fill(uint32_t* out, i64 nblocks4, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nblocks4; t += stride) {
+    Philox4 r = philox4x32_10((uint32_t)t, (uint32_t)(t >> 32), c2, c3, k0, k1);
+    for (int e = 0; e < 4; ++e) out[4 * t + e] = r.v[e];
+  }
+}
+
+namespace {
+i64 ceil_div(i64 a, i64 b) { return (a + b - 1) / b; }
+
+// scan layout in scratch: chunk[nchunks], then one level of tile totals per
+// recursion step (each 1/1024 of the one before)
+size_t scan_bytes(i64 n) {
+  size_t b = 0;
+  while (n > 1) {
+    n = ceil_div(n, 1024);
+    b += (size_t)n * sizeof(double);
+  }
+  return b;
+}
+
+int scan_inplace(double* a, i64 n, double* tmp, cudaStream_t s) {
+  if (n <= 1) return QGB_OK;
+  const i64 tiles = ceil_div(n, 1024);
+  k_scan_tiles<<<(unsigned)tiles, 256, 0, s>>>(a, n, tiles > 1 ? tmp : nullptr);
+  QGB_LAUNCH_CHECK("k_scan_tiles");
+  if (tiles > 1) {
+    int st = scan_inplace(tmp, tiles, tmp + tiles, s);
+    if (st) return st;
+    k_scan_add<<<(unsigned)tiles, 256, 0, s>>>(a, n, tmp);
+    QGB_LAUNCH_CHECK("k_scan_add");
+  }
+  return QGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+size_t qgb_sample_scratch_bytes(int m) {
+  if (m < 0 || m > QGB_MAXQ) return 0;
+  const i64 nchunks = ceil_div((i64)1 << m, QGB_CHUNK);
+  return (size_t)nchunks * sizeof(double) + scan_bytes(nchunks) + 256;
+}
+
+int qgb_sample(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples, int64_t* counts,
+               void* scratch, void* stream) {
+  if (!probs || m < 0 || m > QGB_MAXQ || nshots < 0 || (!samples && !counts) || !scratch) {
+    qgb_set_error("qgb_sample: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  if (nshots == 0) return QGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const i64 nprobs = (i64)1 << m;
+  const i64 nchunks = ceil_div(nprobs, QGB_CHUNK);
+  double* cdf = (double*)scratch;
+  double* tmp = cdf + nchunks;
+  int blocks;
+  grid_for(nchunks, 256, &blocks);
+  k_chunk_sums<<<blocks, 256, 0, s>>>(probs, nprobs, nchunks, cdf);
+  QGB_LAUNCH_CHECK("k_chunk_sums");
+  int st = scan_inplace(cdf, nchunks, tmp, s);
+  if (st) return st;
+  grid_for(nshots, 256, &blocks);
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  if (counts) k_draw<true><<<blocks, 256, 0, s>>>(probs, nprobs, cdf, nchunks, nshots, k0, k1, counts);
+  else k_draw<false><<<blocks, 256, 0, s>>>(probs, nprobs, cdf, nchunks, nshots, k0, k1, samples);
+  QGB_LAUNCH_CHECK("k_draw");
+  return QGB_OK;
+}
+
+// Raw Philox4x32-10 output: out[4*t + e] = word e of philox(ctr = (t_lo,
+// t_hi, c2, c3), key = (k0, k1)) for t < n4 (device pointer; for tests).
+int qgb_philox_fill(uint32_t* out, int64_t n4, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, void* stream) {
+  if (!out || n4 < 0) { qgb_set_error("qgb_philox_fill: bad arguments"); return QGB_ERR_INVALID; }
+  int blocks;
+  grid_for(n4, 256, &blocks);
+  k_philox_fill<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, n4, c2, c3, k0, k1);
+  QGB_LAUNCH_CHECK("k_philox_fill");
+  return QGB_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------- expectation --
+#define QGB_TERMS_PER_LAUNCH 64
+
+struct TermSet {
+  int nterms;
+  u64 zmask[QGB_TERMS_PER_LAUNCH];   // amplitude-index bit masks
+  double coef[QGB_TERMS_PER_LAUNCH];
+  int ny[QGB_TERMS_PER_LAUNCH];      // number of Y factors
+};
+
+// Terms with no X/Y factor: sum_i |psi_i|^2 * sum_t c_t (-1)^popc(i & z_t)
+template <typename T>
+__global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __restrict__ psi, i64 N, TermSet ts,
+                                                     double* __restrict__ part) {
+  double acc = 0.0;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double p = T::abs2(T::load(psi, i));
+    double w = 0.0;
+    for (int t = 0; t < ts.nterms; ++t) w += (__popcll((u64)i & ts.zmask[t]) & 1) ? -ts.coef[t] : ts.coef[t];
+    acc = fma(p, w, acc);
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// Terms sharing flip mask x (highest set bit hb): for each pair (i, j = i^x)
+// with bit hb of i clear, q = conj(psi_i) psi_j and the term adds
+// c * Re(i^ny * (s_j q + s_i conj(q))), s_k = (-1)^popc(k & z).
+template <typename T>
+__global__ void __launch_bounds__(256) k_expect_flip(const typename T::S* __restrict__ psi, i64 npairs, int hb,
+                                                     u64 xmask, TermSet ts, double* __restrict__ part) {
+  double acc = 0.0;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  const i64 low = ((i64)1 << hb) - 1;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < npairs; t += stride) {
+    const i64 i = ((t >> hb) << (hb + 1)) | (t & low);
+    const i64 j = i ^ (i64)xmask;
+    const typename T::V a = T::load(psi, i), b = T::load(psi, j);
+    // q = conj(a) * b
+    const double qr = T::re(a) * T::re(b) + T::im(a) * T::im(b);
+    const double qi = T::re(a) * T::im(b) - T::im(a) * T::re(b);
+    for (int k = 0; k < ts.nterms; ++k) {
+      const double si = (__popcll((u64)i & ts.zmask[k]) & 1) ? -1.0 : 1.0;
+      const double sj = (__popcll((u64)j & ts.zmask[k]) & 1) ? -1.0 : 1.0;
+      // w = s_j q + s_i conj(q)
+      const double wr = (sj + si) * qr, wi = (sj - si) * qi;
+      double v;  // Re(i^ny * w)
+      switch (ts.ny[k] & 3) {
+        case 0: v = wr; break;
+        case 1: v = -wi; break;
+        case 2: v = -wr; break;
+        default: v = wi; break;
+      }
+      acc = fma(ts.coef[k], v, acc);
+    }
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+namespace {
+const int kExpectBlocksCap = 16 * 160;
+
+struct Group {
+  u64 x;
+  std::vector<int> terms;
+};
+
+std::vector<std::pair<Group, int>> expect_plan(int nterms, const uint64_t* xmask, int* nlaunch) {
+  std::map<u64, Group> groups;
+  for (int t = 0; t < nterms; ++t) {
+    Group& g = groups[xmask[t]];
+    g.x = xmask[t];
+    g.terms.push_back(t);
+  }
+  std::vector<std::pair<Group, int>> out;
+  int n = 0;
+  for (auto& kv : groups) {
+    const Group& g = kv.second;
+    for (size_t s = 0; s < g.terms.size(); s += QGB_TERMS_PER_LAUNCH) {
+      Group sub;
+      sub.x = g.x;
+      for (size_t e = s; e < std::min(g.terms.size(), s + QGB_TERMS_PER_LAUNCH); ++e) sub.terms.push_back(g.terms[e]);
+      out.push_back({sub, n++});
+    }
+  }
+  *nlaunch = n;
+  return out;
+}
+
+// qibo qubit mask (bit q = qubit q) -> amplitude-index bit mask
+u64 to_index_mask(u64 qmask, int n) {
+  u64 r = 0;
+  for (int q = 0; q < n; ++q)
+    if ((qmask >> q) & 1) r |= 1ull << (n - 1 - q);
+  return r;
+}
+
+template <typename T>
+int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t* zmask, const double* coef,
+                int nterms, double* out, double* part, cudaStream_t s) {
+  int nlaunch = 0;
+  auto plan = expect_plan(nterms, xmask, &nlaunch);
+  const i64 N = (i64)1 << n;
+  typedef typename T::S S;
+  int used = 0;
+  for (auto& pg : plan) {
+    const Group& g = pg.first;
+    TermSet ts;
+    ts.nterms = (int)g.terms.size();
+    for (int k = 0; k < ts.nterms; ++k) {
+      const int t = g.terms[k];
+      const u64 z = to_index_mask(zmask[t], n), x = to_index_mask(xmask[t], n);
+      ts.zmask[k] = z;
+      ts.coef[k] = coef[t];
+      ts.ny[k] = __builtin_popcountll(z & x);
+    }
+    const u64 x = to_index_mask(g.x, n);
+    int blocks;
+    if (x == 0) {
+      grid_for(N, 256, &blocks);
+      blocks = std::min(blocks, kExpectBlocksCap);
+      k_expect_diag<T><<<blocks, 256, 0, s>>>((const S*)state, N, ts, part + used);
+    } else {
+      const int hb = 63 - __builtin_clzll(x);
+      grid_for(N / 2, 256, &blocks);
+      blocks = std::min(blocks, kExpectBlocksCap);
+      k_expect_flip<T><<<blocks, 256, 0, s>>>((const S*)state, N / 2, hb, x, ts, part + used);
+    }
+    QGB_LAUNCH_CHECK("k_expect");
+    used += blocks;
+  }
+  k_final_sum<<<1, 256, 0, s>>>(part, used, out);
+  QGB_LAUNCH_CHECK("k_final_sum");
+  return QGB_OK;
+}
+}  // namespace
+
+// Dense observable: sum_i conj(psi_i) (H psi)_i, one warp per row of H
+// (complex128, row-major, device).  Backend.expectation_value (:2807-2825).
+template <typename T>
+__global__ void __launch_bounds__(256) k_expect_dense(const typename T::S* __restrict__ psi, i64 N,
+                                                      const double2* __restrict__ H, double* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const i64 warp = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+  const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (i64 row = warp; row < N; row += nwarps) {
+    double hr = 0.0, hi = 0.0;
+    for (i64 j = lane; j < N; j += 32) {
+      const double2 h = H[row * N + j];
+      const typename T::V p = T::load(psi, j);
+      hr += h.x * T::re(p) - h.y * T::im(p);
+      hi += h.x * T::im(p) + h.y * T::re(p);
+    }
+    hr = warp_sum(hr);
+    hi = warp_sum(hi);
+    if (lane == 0) {
+      const typename T::V a = T::load(psi, row);
+      acc += T::re(a) * hr + T::im(a) * hi;  // Re(conj(a) * h)
+    }
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+extern "C" {
+
+int qgb_expect_dense(const void* state, int nqubits, int dtype, const double* hamiltonian, double* out,
+                     void* scratch, void* stream) {
+  if (!state || !hamiltonian || !out || !scratch || nqubits < 1 || nqubits > 20 || !dtype_ok(dtype)) {
+    qgb_set_error("qgb_expect_dense: bad arguments (dense observables up to 20 qubits)");
+    return QGB_ERR_INVALID;
+  }
+  const i64 N = (i64)1 << nqubits;
+  int blocks = (int)std::min<i64>((N + 7) / 8, kExpectBlocksCap);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)scratch;
+  if (dtype == QGB_C128) k_expect_dense<TC128><<<blocks, 256, 0, s>>>((const double2*)state, N, (const double2*)hamiltonian, part);
+  else k_expect_dense<TC64><<<blocks, 256, 0, s>>>((const float2*)state, N, (const double2*)hamiltonian, part);
+  QGB_LAUNCH_CHECK("k_expect_dense");
+  k_final_sum<<<1, 256, 0, s>>>(part, blocks, out);
+  QGB_LAUNCH_CHECK("k_final_sum");
+  return QGB_OK;
+}
+
+size_t qgb_expect_scratch_bytes(int nqubits, int nterms) {
+  (void)nqubits;
+  // at most one launch per term plus one per distinct group
+  return (size_t)(2 * std::max(nterms, 1)) * kExpectBlocksCap * sizeof(double);
+}
+
+int qgb_expect_pauli(const void* state, int nqubits, int dtype, const uint64_t* xmask, const uint64_t* zmask,
+                     const double* coef, int nterms, double* out, void* scratch, void* stream) {
+  if (!state || !out || !scratch || nterms < 0 || (nterms > 0 && (!xmask || !zmask || !coef)) || nqubits < 1 ||
+      nqubits > 63 || !dtype_ok(dtype)) {
+    qgb_set_error("qgb_expect_pauli: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  for (int t = 0; t < nterms; ++t)
+    if ((xmask[t] | zmask[t]) >> nqubits) {
+      qgb_set_error("qgb_expect_pauli: term %d acts on a qubit >= %d", t, nqubits);
+      return QGB_ERR_INVALID;
+    }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nterms == 0) {
+    QGB_TRY_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+    return QGB_OK;
+  }
+  return dtype == QGB_C128 ? expect_impl<TC128>(state, nqubits, xmask, zmask, coef, nterms, out, (double*)scratch, s)
+                           : expect_impl<TC64>(state, nqubits, xmask, zmask, coef, nterms, out, (double*)scratch, s);
+}
+
+}  // extern "C"

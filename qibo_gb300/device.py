@@ -1,0 +1,186 @@
+"""Device runtime: the GPU, its stream, device buffers and state vectors.
+
+A ``DeviceState`` owns a device buffer of ``2**nqubits`` complex amplitudes
+(complex128: 16 B, complex64: 8 B) laid out exactly like the reference's
+numpy state vector (index bit ``n-1-q`` is qubit ``q``).  It quacks like a
+1-D numpy array where qibo's result objects need it (``shape``, ``dtype``,
+``__array__``, ``tolist``), and is copied to the host only when asked.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+import weakref
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_DTYPES = {"complex128": (_lib.QGB_C128, 16), "complex64": (_lib.QGB_C64, 8)}
+
+
+def dtype_code(dtype) -> int:
+    name = np.dtype(dtype).name
+    if name not in _DTYPES:
+        raise TypeError(f"qibo_gb300 states are complex64 or complex128, not {name}")
+    return _DTYPES[name][0]
+
+
+class Runtime:
+    """Process-wide device context: device id, SM count, stream, scratch."""
+
+    _instance = None
+    _lock = threading.Lock()
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        sms = C.c_int(0)
+        check(self.lib.qgb_device_init(device, C.byref(sms)))
+        self.device = device
+        self.sm_count = sms.value
+        self.stream = None  # cudaStream_t handle (int) or None for the legacy default stream
+        self._scratch = None
+        self._scratch_bytes = 0
+
+    @classmethod
+    def get(cls) -> "Runtime":
+        with cls._lock:
+            if cls._instance is None:
+                cls._instance = Runtime()
+            return cls._instance
+
+    # -- memory ---------------------------------------------------------
+    def malloc(self, nbytes: int) -> int:
+        p = C.c_void_p()
+        check(self.lib.qgb_malloc(C.byref(p), int(nbytes)))
+        return p.value or 0
+
+    def free(self, ptr: int):
+        if ptr:
+            self.lib.qgb_free(C.c_void_p(ptr))
+
+    def scratch(self, nbytes: int) -> int:
+        """A grow-only scratch buffer shared by stream-ordered calls."""
+        if nbytes <= 0:
+            return 0
+        if nbytes > self._scratch_bytes:
+            if self._scratch:
+                self.synchronize()
+                self.free(self._scratch)
+                self._scratch = None
+            self._scratch = self.malloc(nbytes)
+            self._scratch_bytes = nbytes
+        return self._scratch
+
+    def synchronize(self):
+        check(self.lib.qgb_stream_sync(self.stream))
+
+    def mem_info(self):
+        f, t = C.c_size_t(), C.c_size_t()
+        check(self.lib.qgb_mem_info(C.byref(f), C.byref(t)))
+        return f.value, t.value
+
+    def h2d(self, dst: int, arr: np.ndarray):
+        arr = np.ascontiguousarray(arr)
+        check(self.lib.qgb_memcpy_h2d(dst, arr.ctypes.data, arr.nbytes, self.stream))
+        self.synchronize()  # the host array may be released after return
+
+    def d2h(self, arr: np.ndarray, src: int):
+        check(self.lib.qgb_memcpy_d2h(arr.ctypes.data, src, arr.nbytes, self.stream))
+        self.synchronize()
+
+
+class DeviceArray:
+    """A plain device array (e.g. FP64 probabilities, int64 counts)."""
+
+    def __init__(self, shape, dtype, rt: Runtime | None = None, ptr: int | None = None, owner=None):
+        self.rt = rt or Runtime.get()
+        self.shape = tuple(int(s) for s in (shape if isinstance(shape, (tuple, list)) else (shape,)))
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self._owner = owner
+        if ptr is None:
+            self.ptr = self.rt.malloc(max(self.nbytes, 1))
+            self._fin = weakref.finalize(self, self.rt.free, self.ptr)
+        else:
+            self.ptr = ptr
+            self._fin = None
+
+    @property
+    def ndim(self):
+        return len(self.shape)
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+    def __len__(self):
+        return self.shape[0]
+
+    def to_numpy(self) -> np.ndarray:
+        out = np.empty(self.shape, dtype=self.dtype)
+        if self.nbytes:
+            self.rt.d2h(out, self.ptr)
+        return out
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.to_numpy()
+        return a if dtype is None else a.astype(dtype)
+
+    def tolist(self):
+        return self.to_numpy().tolist()
+
+    def __getitem__(self, item):
+        return self.to_numpy()[item]
+
+    def __repr__(self):
+        return f"DeviceArray(shape={self.shape}, dtype={self.dtype.name})"
+
+    def free(self):
+        if self._fin is not None:
+            self._fin()
+
+
+class DeviceState(DeviceArray):
+    """State vector of ``nqubits`` qubits resident in device memory."""
+
+    def __init__(self, nqubits: int, dtype="complex128", rt: Runtime | None = None, ptr: int | None = None):
+        self.nqubits = int(nqubits)
+        self.code = dtype_code(dtype)
+        super().__init__((2**self.nqubits,), dtype, rt, ptr)
+
+    # -- creation ---------------------------------------------------------
+    @classmethod
+    def zero(cls, nqubits: int, dtype="complex128") -> "DeviceState":
+        st = cls(nqubits, dtype)
+        check(st.rt.lib.qgb_state_zero(st.ptr, st.nqubits, st.code, st.rt.stream))
+        return st
+
+    @classmethod
+    def from_numpy(cls, arr, dtype=None) -> "DeviceState":
+        arr = np.asarray(arr)
+        if arr.ndim != 1 or arr.shape[0] & (arr.shape[0] - 1) or arr.shape[0] < 2:
+            raise ValueError(f"a state vector has shape (2**n,), got {arr.shape}")
+        dtype = np.dtype(dtype or (arr.dtype if arr.dtype in (np.complex64, np.complex128) else np.complex128))
+        n = int(arr.shape[0]).bit_length() - 1
+        st = cls(n, dtype)
+        st.rt.h2d(st.ptr, arr.astype(dtype, copy=False))
+        return st
+
+    def copy(self) -> "DeviceState":
+        out = DeviceState(self.nqubits, self.dtype, self.rt)
+        check(self.rt.lib.qgb_memcpy_d2d(out.ptr, self.ptr, self.nbytes, self.rt.stream))
+        return out
+
+    def astype(self, dtype, copy: bool = True) -> "DeviceState":
+        dtype = np.dtype(dtype)
+        if dtype == self.dtype:
+            return self.copy() if copy else self
+        out = DeviceState(self.nqubits, dtype, self.rt)
+        check(self.rt.lib.qgb_state_cast(self.ptr, self.code, out.ptr, out.code, self.nqubits, self.rt.stream))
+        return out
+
+    def __repr__(self):
+        return f"DeviceState(nqubits={self.nqubits}, dtype={self.dtype.name})"

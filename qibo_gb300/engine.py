@@ -1,0 +1,138 @@
+"""Thin host-side driver of the C-ABI: gates, probabilities, sampling and
+expectations on ``DeviceState`` objects.
+
+Gate descriptors are ``(qubits, controls, matrix)``: ``qubits`` in matrix
+order (``qubits[0]`` is the most significant matrix-index bit, the order of
+the reference's ``gate.qubits``), ``controls`` the ``controlled_by`` qubits
+(the matrix then acts on ``qubits`` only where all controls are 1,
+backends/abstract.py:3176-3197), ``matrix`` a complex 2^k x 2^k array.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, List, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import QgbOp, check, double_array, int_array
+from .device import DeviceArray, DeviceState, Runtime
+
+GateDesc = Tuple[Sequence[int], Sequence[int], np.ndarray]
+
+
+def _matrix_doubles(m) -> np.ndarray:
+    m = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+    return m.view(np.float64).ravel()
+
+
+class Engine:
+    def __init__(self, rt: Runtime | None = None):
+        self.rt = rt or Runtime.get()
+        self.lib = self.rt.lib
+
+    # -- gates -----------------------------------------------------------
+    def apply(self, state: DeviceState, qubits: Sequence[int], matrix, controls: Sequence[int] = ()):
+        qubits, controls = list(qubits), list(controls)
+        m = _matrix_doubles(matrix)
+        if m.size != 2 * 4 ** len(qubits):
+            raise ValueError(f"matrix of {m.size // 2} entries for {len(qubits)} qubits")
+        check(self.lib.qgb_apply_gate(state.ptr, state.nqubits, state.code, int_array(qubits), len(qubits),
+                                      int_array(controls), len(controls),
+                                      m.ctypes.data_as(_lib.dp), self.rt.stream))
+
+    def apply_many(self, state: DeviceState, descs: Iterable[GateDesc], blocked: bool = False):
+        """Apply a gate list with one C call (``qgb_apply_circuit``)."""
+        descs = list(descs)
+        if not descs:
+            return
+        ops = (QgbOp * len(descs))()
+        coefs: List[np.ndarray] = []
+        off = 0
+        for i, (qubits, controls, matrix) in enumerate(descs):
+            qubits, controls = list(qubits), list(controls)
+            if len(qubits) > 5 or len(controls) > 8:
+                raise NotImplementedError(f"gate on {len(qubits)} qubits with {len(controls)} controls")
+            m = _matrix_doubles(matrix)
+            if m.size != 2 * 4 ** len(qubits):
+                raise ValueError(f"matrix of {m.size // 2} entries for {len(qubits)} qubits")
+            op = ops[i]
+            op.k = len(qubits)
+            op.ncontrols = len(controls)
+            for j, q in enumerate(qubits):
+                op.qubits[j] = q
+            for j, q in enumerate(controls):
+                op.controls[j] = q
+            op.coef_offset = off
+            coefs.append(m)
+            off += m.size
+        allc = np.concatenate(coefs)
+        check(self.lib.qgb_apply_circuit(state.ptr, state.nqubits, state.code, ops, len(descs),
+                                         allc.ctypes.data_as(_lib.dp),
+                                         _lib.QGB_PLAN_BLOCKED if blocked else 0, self.rt.stream))
+
+    # -- reductions -------------------------------------------------------
+    def probabilities(self, state: DeviceState, qubits: Sequence[int]) -> DeviceArray:
+        """Marginal probabilities (FP64, device) of ``qubits`` in that order."""
+        qubits = list(qubits)
+        out = DeviceArray((2 ** len(qubits),), np.float64, self.rt)
+        nbytes = self.lib.qgb_probs_scratch_bytes(state.nqubits, len(qubits))
+        scratch = self.rt.scratch(nbytes)
+        check(self.lib.qgb_probabilities(state.ptr, state.nqubits, state.code, int_array(qubits), len(qubits),
+                                         out.ptr, scratch or None, self.rt.stream))
+        return out
+
+    def norm2(self, state: DeviceState) -> float:
+        out = DeviceArray((1,), np.float64, self.rt)
+        scratch = self.rt.scratch(self.lib.qgb_norm_scratch_bytes())
+        check(self.lib.qgb_norm2(state.ptr, state.nqubits, state.code, out.ptr, scratch, self.rt.stream))
+        return float(out.to_numpy()[0])
+
+    def scale(self, state: DeviceState, factor: float):
+        check(self.lib.qgb_state_scale(state.ptr, state.nqubits, state.code, float(factor), self.rt.stream))
+
+    def sample(self, probs: DeviceArray, nshots: int, seed: int, counts: bool = True) -> np.ndarray:
+        """Draw ``nshots`` outcomes from device FP64 ``probs`` (length 2^m).
+
+        Returns host int64 counts (length 2^m) or samples (length nshots)."""
+        m = int(probs.shape[0]).bit_length() - 1
+        if 2**m != probs.shape[0]:
+            raise ValueError("probability vector length must be a power of two")
+        scratch = self.rt.scratch(self.lib.qgb_sample_scratch_bytes(m))
+        if counts:
+            out = DeviceArray((2**m,), np.int64, self.rt)
+            check(self.lib.qgb_memset_zero(out.ptr, out.nbytes, self.rt.stream))
+            check(self.lib.qgb_sample(probs.ptr, m, int(nshots), int(seed) & (2**64 - 1), None, out.ptr,
+                                      scratch, self.rt.stream))
+        else:
+            out = DeviceArray((int(nshots),), np.int64, self.rt)
+            check(self.lib.qgb_sample(probs.ptr, m, int(nshots), int(seed) & (2**64 - 1), out.ptr, None,
+                                      scratch, self.rt.stream))
+        return out.to_numpy()
+
+    def expect_pauli(self, state: DeviceState, xmask: Sequence[int], zmask: Sequence[int],
+                     coef: Sequence[float]) -> float:
+        """sum_t coef[t] <psi|P_t|psi>, P_t given by qubit bit masks (bit q = qubit q)."""
+        n = len(coef)
+        xm = (C.c_uint64 * max(1, n))(*[int(x) for x in xmask])
+        zm = (C.c_uint64 * max(1, n))(*[int(z) for z in zmask])
+        cf = double_array(coef)
+        out = DeviceArray((1,), np.float64, self.rt)
+        scratch = self.rt.scratch(self.lib.qgb_expect_scratch_bytes(state.nqubits, n))
+        check(self.lib.qgb_expect_pauli(state.ptr, state.nqubits, state.code, xm, zm, cf, n, out.ptr, scratch,
+                                        self.rt.stream))
+        return float(out.to_numpy()[0])
+
+
+def pauli_masks(term: str, qubits: Sequence[int]) -> Tuple[int, int]:
+    """(xmask, zmask) of a Pauli string such as ``"XZY"`` on ``qubits``."""
+    x = z = 0
+    for f, q in zip(term, qubits):
+        if f in ("X", "Y"):
+            x |= 1 << q
+        if f in ("Z", "Y"):
+            z |= 1 << q
+        if f not in ("X", "Y", "Z", "I"):
+            raise ValueError(f"unknown Pauli factor {f!r}")
+    return x, z
