@@ -21,9 +21,7 @@
 #include <cstring>
 #include <vector>
 
-#include "qgb_common.cuh"
-
-typedef std::complex<double> zd;
+#include "qgb_plan.h"
 
 template <int K>
 struct Offs { i64 o[1 << K]; };
@@ -175,33 +173,6 @@ __global__ void __launch_bounds__(256) k_swap(typename T::S* __restrict__ psi, i
 // host side
 namespace {
 
-struct Geometry {
-  int n;
-  std::vector<int> tbits;   // target bit positions, matrix order
-  std::vector<int> cbits;   // control bit positions
-};
-
-int validate(void* state, int n, int dtype, const int* qubits, int k, const int* controls, int nc,
-             const char* fn, Geometry* g) {
-  if (!state) { qgb_set_error("%s: null state", fn); return QGB_ERR_INVALID; }
-  if (n < 1 || n > QGB_MAXQ) { qgb_set_error("%s: nqubits=%d out of range", fn, n); return QGB_ERR_INVALID; }
-  if (!dtype_ok(dtype)) { qgb_set_error("%s: unknown dtype %d", fn, dtype); return QGB_ERR_INVALID; }
-  if (k < 0 || k > QGB_MAX_K) { qgb_set_error("%s: %d target qubits (max %d)", fn, k, QGB_MAX_K); return QGB_ERR_UNSUPPORTED; }
-  if (nc < 0 || nc > QGB_MAX_CTRL) { qgb_set_error("%s: %d controls (max %d)", fn, nc, QGB_MAX_CTRL); return QGB_ERR_UNSUPPORTED; }
-  u64 seen = 0;
-  g->n = n;
-  g->tbits.clear();
-  g->cbits.clear();
-  for (int j = 0; j < k + nc; ++j) {
-    int q = j < k ? qubits[j] : controls[j - k];
-    if (q < 0 || q >= n) { qgb_set_error("%s: qubit %d out of range for %d qubits", fn, q, n); return QGB_ERR_INVALID; }
-    if (seen & (1ull << q)) { qgb_set_error("%s: qubit %d repeated", fn, q); return QGB_ERR_INVALID; }
-    seen |= 1ull << q;
-    (j < k ? g->tbits : g->cbits).push_back(n - 1 - q);
-  }
-  return QGB_OK;
-}
-
 BitInsert make_insert(std::vector<int> bits) {
   BitInsert bi;
   std::sort(bits.begin(), bits.end());
@@ -217,22 +188,23 @@ i64 mask_of(const std::vector<int>& bits) {
 }
 
 template <typename T>
-int launch_dense(void* state, const Geometry& g, const std::vector<zd>& M, cudaStream_t s) {
+int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
   const int k = (int)g.tbits.size();
   std::vector<int> fixed = g.tbits;
   fixed.insert(fixed.end(), g.cbits.begin(), g.cbits.end());
   BitInsert bi = make_insert(fixed);
   const i64 cmask = mask_of(g.cbits);
-  const i64 ngroups = (i64)1 << (g.n - (int)fixed.size());
+  const i64 ngroups = (i64)1 << (n - (int)fixed.size());
   const int D = 1 << k;
+  const std::vector<zd>& M = g.coef;
   typedef typename T::S S;
   // fast 1-qubit paths (no controls)
   if (k == 1 && g.cbits.empty()) {
     const int b = g.tbits[0];
     typename T::V u00 = T::coef(M[0].real(), M[0].imag()), u01 = T::coef(M[1].real(), M[1].imag());
     typename T::V u10 = T::coef(M[2].real(), M[2].imag()), u11 = T::coef(M[3].real(), M[3].imag());
-    if (b < 5 && g.n >= 5) {
-      const i64 N = (i64)1 << g.n;
+    if (b < 5 && n >= 5) {
+      const i64 N = (i64)1 << n;
       int blocks;
       grid_for(N, 256, &blocks);
       k_1q_shfl<T><<<blocks, 256, 0, s>>>((S*)state, N, b, u00, u01, u10, u11);
@@ -249,21 +221,21 @@ int launch_dense(void* state, const Geometry& g, const std::vector<zd>& M, cudaS
   }
   int blocks;
   grid_for(ngroups, 256, &blocks);
-#define QGB_DENSE_CASE(KK)                                                              \
-  case KK: {                                                                            \
-    Offs<KK> off;                                                                       \
-    DenseMat<T, KK> dm;                                                                 \
-    for (int m = 0; m < D; ++m) {                                                       \
-      i64 o = 0;                                                                        \
-      for (int j = 0; j < k; ++j)                                                       \
-        if ((m >> (k - 1 - j)) & 1) o |= (i64)1 << g.tbits[j];                          \
-      off.o[m] = o;                                                                     \
-    }                                                                                   \
-    for (int r = 0; r < D; ++r)                                                         \
+#define QGB_DENSE_CASE(KK)                                                                        \
+  case KK: {                                                                                      \
+    Offs<KK> off;                                                                                 \
+    DenseMat<T, KK> dm;                                                                           \
+    for (int m = 0; m < D; ++m) {                                                                 \
+      i64 o = 0;                                                                                  \
+      for (int j = 0; j < k; ++j)                                                                 \
+        if ((m >> (k - 1 - j)) & 1) o |= (i64)1 << g.tbits[j];                                    \
+      off.o[m] = o;                                                                               \
+    }                                                                                             \
+    for (int r = 0; r < D; ++r)                                                                   \
       for (int c = 0; c < D; ++c) dm.m[r][c] = T::coef(M[r * D + c].real(), M[r * D + c].imag()); \
-    k_dense<T, KK><<<blocks, 256, 0, s>>>((S*)state, ngroups, bi, cmask, off, dm);      \
-    QGB_LAUNCH_CHECK("k_dense");                                                        \
-    return QGB_OK;                                                                      \
+    k_dense<T, KK><<<blocks, 256, 0, s>>>((S*)state, ngroups, bi, cmask, off, dm);                \
+    QGB_LAUNCH_CHECK("k_dense");                                                                  \
+    return QGB_OK;                                                                                \
   }
   switch (k) {
     QGB_DENSE_CASE(1)
@@ -291,14 +263,14 @@ int launch_phase(void* state, int n, const std::vector<int>& bits, zd ph, cudaSt
 }
 
 template <typename T>
-int launch_diag(void* state, const Geometry& g, const std::vector<zd>& d, cudaStream_t s) {
+int launch_diag(void* state, int n, const GateOp& g, cudaStream_t s) {
   const int k = (int)g.tbits.size();
   BitInsert bi = make_insert(g.cbits);
-  const i64 count = (i64)1 << (g.n - (int)g.cbits.size());
+  const i64 count = (i64)1 << (n - (int)g.cbits.size());
   Offs<QGB_MAX_K> tb;
   for (int j = 0; j < QGB_MAX_K; ++j) tb.o[j] = j < k ? g.tbits[j] : 0;
   DiagVec<T> D;
-  for (int m = 0; m < 32; ++m) D.d[m] = m < (1 << k) ? T::coef(d[m].real(), d[m].imag()) : T::coef(1.0, 0.0);
+  for (int m = 0; m < 32; ++m) D.d[m] = m < (1 << k) ? T::coef(g.coef[m].real(), g.coef[m].imag()) : T::coef(1.0, 0.0);
   int blocks;
   grid_for(count, 256, &blocks);
   k_diagk<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), k, tb, D);
@@ -307,13 +279,14 @@ int launch_diag(void* state, const Geometry& g, const std::vector<zd>& d, cudaSt
 }
 
 template <typename T>
-int launch_xlike(void* state, const Geometry& g, zd a, zd b, cudaStream_t s) {
+int launch_xlike(void* state, int n, const GateOp& g, cudaStream_t s) {
   std::vector<int> fixed = g.cbits;
   fixed.push_back(g.tbits[0]);
   BitInsert bi = make_insert(fixed);
-  const i64 count = (i64)1 << (g.n - (int)fixed.size());
+  const i64 count = (i64)1 << (n - (int)fixed.size());
   int blocks;
   grid_for(count, 256, &blocks);
+  const zd a = g.coef[0], b = g.coef[1];
   const int plain = (a == zd(1, 0) && b == zd(1, 0)) ? 1 : 0;
   k_xlike<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), (i64)1 << g.tbits[0],
                                     T::coef(a.real(), a.imag()), T::coef(b.real(), b.imag()), plain);
@@ -322,12 +295,12 @@ int launch_xlike(void* state, const Geometry& g, zd a, zd b, cudaStream_t s) {
 }
 
 template <typename T>
-int launch_swap(void* state, const Geometry& g, cudaStream_t s) {
+int launch_swap(void* state, int n, const GateOp& g, cudaStream_t s) {
   std::vector<int> fixed = g.cbits;
   fixed.push_back(g.tbits[0]);
   fixed.push_back(g.tbits[1]);
   BitInsert bi = make_insert(fixed);
-  const i64 count = (i64)1 << (g.n - (int)fixed.size());
+  const i64 count = (i64)1 << (n - (int)fixed.size());
   int blocks;
   grid_for(count, 256, &blocks);
   k_swap<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(g.cbits), (i64)1 << g.tbits[0],
@@ -336,12 +309,24 @@ int launch_swap(void* state, const Geometry& g, cudaStream_t s) {
   return QGB_OK;
 }
 
-// Move target j of (g, M) into the controls when the matrix is the identity
-// on the subspace where that qubit is 0 and does not couple it to the 1
-// subspace.  Returns true when a control was extracted.
-bool extract_control(Geometry& g, std::vector<zd>& M) {
+template <typename T>
+int launch_op(void* state, int n, const GateOp& g, cudaStream_t s) {
+  if (g.identity) return QGB_OK;
+  switch (g.kind) {
+    case GK_PHASE: return launch_phase<T>(state, n, g.cbits, g.coef[0], s);
+    case GK_DIAG: return launch_diag<T>(state, n, g, s);
+    case GK_XLIKE: return launch_xlike<T>(state, n, g, s);
+    case GK_SWAP: return launch_swap<T>(state, n, g, s);
+    default: return launch_dense<T>(state, n, g, s);
+  }
+}
+
+// Move a target into the controls when the matrix is the identity on the
+// subspace where that qubit is 0 and does not couple it to the 1 subspace.
+bool extract_control(GateOp& g) {
   const int k = (int)g.tbits.size();
   const int D = 1 << k;
+  std::vector<zd>& M = g.coef;
   for (int j = 0; j < k; ++j) {
     const int bit = 1 << (k - 1 - j);
     bool ok = true;
@@ -352,7 +337,6 @@ bool extract_control(Geometry& g, std::vector<zd>& M) {
         if (M[r * D + c] != want) ok = false;
       }
     if (!ok) continue;
-    // keep rows/cols with the bit set
     std::vector<zd> R((D / 2) * (D / 2));
     int ri = 0;
     for (int r = 0; r < D; ++r) {
@@ -373,103 +357,172 @@ bool extract_control(Geometry& g, std::vector<zd>& M) {
   return false;
 }
 
-template <typename T>
-int dispatch(void* state, Geometry g, std::vector<zd> M, cudaStream_t s) {
-  while (!g.tbits.empty() && extract_control(g, M)) {
+}  // namespace
+
+int qgb_classify(int n, const int* qubits, int k, const int* controls, int nc, const double* matrix, GateOp* op,
+                 const char* fn) {
+  if (n < 1 || n > QGB_MAXQ) { qgb_set_error("%s: nqubits=%d out of range", fn, n); return QGB_ERR_INVALID; }
+  if (k < 0 || k > QGB_MAX_K) { qgb_set_error("%s: %d target qubits (max %d)", fn, k, QGB_MAX_K); return QGB_ERR_UNSUPPORTED; }
+  if (nc < 0 || nc > QGB_MAX_CTRL) { qgb_set_error("%s: %d controls (max %d)", fn, nc, QGB_MAX_CTRL); return QGB_ERR_UNSUPPORTED; }
+  if (!matrix && k > 0) { qgb_set_error("%s: null matrix", fn); return QGB_ERR_INVALID; }
+  u64 seen = 0;
+  GateOp& g = *op;
+  g = GateOp();
+  for (int j = 0; j < k + nc; ++j) {
+    const int q = j < k ? qubits[j] : controls[j - k];
+    if (q < 0 || q >= n) { qgb_set_error("%s: qubit %d out of range for %d qubits", fn, q, n); return QGB_ERR_INVALID; }
+    if (seen & (1ull << q)) { qgb_set_error("%s: qubit %d repeated", fn, q); return QGB_ERR_INVALID; }
+    seen |= 1ull << q;
+    (j < k ? g.tbits : g.cbits).push_back(n - 1 - q);
   }
-  const int k = (int)g.tbits.size();
   const int D = 1 << k;
-  if (k == 0) return launch_phase<T>(state, g.n, g.cbits, M[0], s);
-  bool diag = true, offdiag1 = (k == 1);
-  for (int r = 0; r < D; ++r)
-    for (int c = 0; c < D; ++c) {
-      if (r != c && M[r * D + c] != zd(0, 0)) diag = false;
-      if (k == 1 && r == c && M[r * D + c] != zd(0, 0)) offdiag1 = false;
+  g.coef.resize(D * D);
+  for (int i = 0; i < D * D; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
+  while (!g.tbits.empty() && extract_control(g)) {
+  }
+  const int kk = (int)g.tbits.size();
+  const int DD = 1 << kk;
+  if (kk == 0) {
+    g.kind = GK_PHASE;
+    g.identity = g.coef[0] == zd(1, 0);
+    return QGB_OK;
+  }
+  bool diag = true, anti = (kk == 1);
+  for (int r = 0; r < DD; ++r)
+    for (int c = 0; c < DD; ++c) {
+      if (r != c && g.coef[r * DD + c] != zd(0, 0)) diag = false;
+      if (kk == 1 && r == c && g.coef[r * DD + c] != zd(0, 0)) anti = false;
     }
   if (diag) {
-    // diag(1, ..., 1, phase) with a single target was caught as a control;
-    // a diagonal with a unit first entry on one target is a phase on its 1s
-    if (k == 1 && M[0] == zd(1, 0)) {
-      std::vector<int> bits = g.cbits;
-      bits.push_back(g.tbits[0]);
-      return launch_phase<T>(state, g.n, bits, M[3], s);
+    if (kk == 1 && g.coef[0] == zd(1, 0)) {  // phase on the target's 1s
+      const zd ph = g.coef[3];
+      g.cbits.push_back(g.tbits[0]);
+      g.tbits.clear();
+      g.kind = GK_PHASE;
+      g.coef = {ph};
+      g.identity = ph == zd(1, 0);
+      return QGB_OK;
     }
-    std::vector<zd> d(D);
-    for (int m = 0; m < D; ++m) d[m] = M[m * D + m];
-    return launch_diag<T>(state, g, d, s);
+    std::vector<zd> d(DD);
+    for (int m = 0; m < DD; ++m) d[m] = g.coef[m * DD + m];
+    g.kind = GK_DIAG;
+    g.coef = d;
+    return QGB_OK;
   }
-  if (offdiag1) return launch_xlike<T>(state, g, M[1], M[2], s);
-  if (k == 2) {
+  if (anti) {
+    g.kind = GK_XLIKE;
+    g.coef = {g.coef[1], g.coef[2]};
+    return QGB_OK;
+  }
+  if (kk == 2) {
     const zd one(1, 0), zero(0, 0);
     const zd sw[16] = {one, zero, zero, zero, zero, zero, one, zero, zero, one, zero, zero, zero, zero, zero, one};
     bool is_swap = true;
     for (int i = 0; i < 16; ++i)
-      if (M[i] != sw[i]) is_swap = false;
-    if (is_swap) return launch_swap<T>(state, g, s);
+      if (g.coef[i] != sw[i]) is_swap = false;
+    if (is_swap) {
+      g.kind = GK_SWAP;
+      g.coef.clear();
+      return QGB_OK;
+    }
   }
-  return launch_dense<T>(state, g, M, s);
+  g.kind = GK_DENSE;
+  return QGB_OK;
 }
 
-std::vector<zd> read_matrix(const double* m, int k) {
-  const int D = 1 << k;
-  std::vector<zd> M(D * D);
-  for (int i = 0; i < D * D; ++i) M[i] = zd(m[2 * i], m[2 * i + 1]);
-  return M;
+namespace {
+int check_state_args(void* state, int dtype, const char* fn) {
+  if (!state) { qgb_set_error("%s: null state", fn); return QGB_ERR_INVALID; }
+  if (!dtype_ok(dtype)) { qgb_set_error("%s: unknown dtype %d", fn, dtype); return QGB_ERR_INVALID; }
+  return QGB_OK;
 }
 
+int launch_any(void* state, int n, int dtype, const GateOp& g, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == QGB_C128 ? launch_op<TC128>(state, n, g, s) : launch_op<TC64>(state, n, g, s);
+}
 }  // namespace
+
+int qgb_launch_gateop(void* state, int n, int dtype, const GateOp& g, cudaStream_t s) {
+  return launch_any(state, n, dtype, g, (void*)s);
+}
 
 extern "C" {
 
 int qgb_apply_gate(void* state, int nqubits, int dtype, const int* qubits, int k, const int* controls,
                    int ncontrols, const double* matrix, void* stream) {
-  Geometry g;
-  int st = validate(state, nqubits, dtype, qubits, k, controls, ncontrols, "qgb_apply_gate", &g);
+  int st = check_state_args(state, dtype, "qgb_apply_gate");
   if (st) return st;
-  if (!matrix) { qgb_set_error("qgb_apply_gate: null matrix"); return QGB_ERR_INVALID; }
-  std::vector<zd> M = read_matrix(matrix, k);
-  cudaStream_t s = (cudaStream_t)stream;
-  return dtype == QGB_C128 ? dispatch<TC128>(state, g, M, s) : dispatch<TC64>(state, g, M, s);
+  GateOp g;
+  st = qgb_classify(nqubits, qubits, k, controls, ncontrols, matrix, &g, "qgb_apply_gate");
+  if (st) return st;
+  return launch_any(state, nqubits, dtype, g, stream);
 }
 
 int qgb_apply_1q(void* state, int nqubits, int dtype, int target, const double* matrix, void* stream) {
-  Geometry g;
-  int st = validate(state, nqubits, dtype, &target, 1, nullptr, 0, "qgb_apply_1q", &g);
+  int st = check_state_args(state, dtype, "qgb_apply_1q");
   if (st) return st;
-  std::vector<zd> M = read_matrix(matrix, 1);
-  cudaStream_t s = (cudaStream_t)stream;
-  return dtype == QGB_C128 ? launch_dense<TC128>(state, g, M, s) : launch_dense<TC64>(state, g, M, s);
+  GateOp g;
+  st = qgb_classify(nqubits, &target, 0, nullptr, 0, nullptr, &g, "qgb_apply_1q");  // validation only
+  if (st) return st;
+  if (target < 0 || target >= nqubits || !matrix) { qgb_set_error("qgb_apply_1q: bad target or matrix"); return QGB_ERR_INVALID; }
+  g.kind = GK_DENSE;
+  g.tbits = {nqubits - 1 - target};
+  g.cbits.clear();
+  g.coef.resize(4);
+  for (int i = 0; i < 4; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
+  return launch_any(state, nqubits, dtype, g, stream);
 }
 
 int qgb_apply_2q(void* state, int nqubits, int dtype, int q0, int q1, const double* matrix, void* stream) {
-  Geometry g;
-  int qs[2] = {q0, q1};
-  int st = validate(state, nqubits, dtype, qs, 2, nullptr, 0, "qgb_apply_2q", &g);
+  int st = check_state_args(state, dtype, "qgb_apply_2q");
   if (st) return st;
-  std::vector<zd> M = read_matrix(matrix, 2);
-  cudaStream_t s = (cudaStream_t)stream;
-  return dtype == QGB_C128 ? launch_dense<TC128>(state, g, M, s) : launch_dense<TC64>(state, g, M, s);
+  const int qs[2] = {q0, q1};
+  GateOp g;
+  st = qgb_classify(nqubits, qs, 0, qs, 2, nullptr, &g, "qgb_apply_2q");  // range/duplicate checks
+  if (st) return st;
+  if (!matrix) { qgb_set_error("qgb_apply_2q: null matrix"); return QGB_ERR_INVALID; }
+  g = GateOp();
+  g.kind = GK_DENSE;
+  g.tbits = {nqubits - 1 - q0, nqubits - 1 - q1};
+  g.coef.resize(16);
+  for (int i = 0; i < 16; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
+  return launch_any(state, nqubits, dtype, g, stream);
 }
 
 int qgb_apply_phase(void* state, int nqubits, int dtype, const int* qubits, int nq, double phase_re,
                     double phase_im, void* stream) {
-  Geometry g;
-  int st = validate(state, nqubits, dtype, nullptr, 0, qubits, nq, "qgb_apply_phase", &g);
+  int st = check_state_args(state, dtype, "qgb_apply_phase");
   if (st) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  zd ph(phase_re, phase_im);
-  return dtype == QGB_C128 ? launch_phase<TC128>(state, nqubits, g.cbits, ph, s)
-                           : launch_phase<TC64>(state, nqubits, g.cbits, ph, s);
+  GateOp g;
+  st = qgb_classify(nqubits, nullptr, 0, qubits, nq, nullptr, &g, "qgb_apply_phase");
+  if (st) return st;
+  g.kind = GK_PHASE;
+  g.coef = {zd(phase_re, phase_im)};
+  g.identity = g.coef[0] == zd(1, 0);
+  return launch_any(state, nqubits, dtype, g, stream);
 }
 
 int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1, const int* controls, int ncontrols,
                    void* stream) {
-  Geometry g;
-  int qs[2] = {q0, q1};
-  int st = validate(state, nqubits, dtype, qs, 2, controls, ncontrols, "qgb_apply_swap", &g);
+  int st = check_state_args(state, dtype, "qgb_apply_swap");
   if (st) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  return dtype == QGB_C128 ? launch_swap<TC128>(state, g, s) : launch_swap<TC64>(state, g, s);
+  const int qs[2] = {q0, q1};
+  GateOp g;
+  st = qgb_classify(nqubits, qs, 0, nullptr, 0, nullptr, &g, "qgb_apply_swap");
+  if (st) return st;
+  GateOp c;
+  st = qgb_classify(nqubits, controls, 0, qs, 2, nullptr, &c, "qgb_apply_swap");  // overlap checks
+  if (st) return st;
+  std::vector<int> all(qs, qs + 2);
+  for (int i = 0; i < ncontrols; ++i) all.push_back(controls[i]);
+  st = qgb_classify(nqubits, nullptr, 0, all.data(), (int)all.size(), nullptr, &c, "qgb_apply_swap");
+  if (st) return st;
+  g = GateOp();
+  g.kind = GK_SWAP;
+  g.tbits = {nqubits - 1 - q0, nqubits - 1 - q1};
+  for (int i = 0; i < ncontrols; ++i) g.cbits.push_back(nqubits - 1 - controls[i]);
+  return launch_any(state, nqubits, dtype, g, stream);
 }
 
 }  // extern "C"
@@ -482,12 +535,17 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
 extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                                  const double* coefs, int flags, void* stream) {
   if (nops < 0 || (nops > 0 && (!ops || !coefs))) { qgb_set_error("qgb_apply_circuit: bad arguments"); return QGB_ERR_INVALID; }
+  int st = check_state_args(state, dtype, "qgb_apply_circuit");
+  if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   if (flags & QGB_PLAN_BLOCKED) return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, s);
   for (int i = 0; i < nops; ++i) {
     const qgb_op& op = ops[i];
-    int st = qgb_apply_gate(state, nqubits, dtype, op.qubits, op.k, op.controls, op.ncontrols,
-                            coefs + op.coef_offset, stream);
+    GateOp g;
+    st = qgb_classify(nqubits, op.qubits, op.k, op.controls, op.ncontrols, coefs + op.coef_offset, &g,
+                      "qgb_apply_circuit");
+    if (st) return st;
+    st = launch_any(state, nqubits, dtype, g, stream);
     if (st) return st;
   }
   return QGB_OK;

@@ -1,0 +1,32 @@
+// Host-side gate classification shared by the per-gate dispatcher and the
+// shared-memory pass planner.
+#pragma once
+
+#include <complex>
+#include <vector>
+
+#include "qgb_common.cuh"
+
+typedef std::complex<double> zd;
+
+enum GateKind {
+  GK_PHASE = 0,  // amplitudes with all ``cbits`` set get *coef[0]
+  GK_DIAG = 1,   // amplitude *= coef[target bits] where all ``cbits`` set
+  GK_XLIKE = 2,  // [[0, a], [b, 0]] on tbits[0] where all ``cbits`` set
+  GK_SWAP = 3,   // SWAP of tbits[0], tbits[1] where all ``cbits`` set
+  GK_DENSE = 4,  // dense 2^k x 2^k on tbits where all ``cbits`` set
+};
+
+struct GateOp {
+  int kind;
+  std::vector<int> tbits;  // target bit positions, most significant matrix bit first
+  std::vector<int> cbits;  // control bit positions (all must be 1)
+  std::vector<zd> coef;    // PHASE: 1; DIAG: 2^k; XLIKE: 2 (a, b); SWAP: 0; DENSE: 4^k row-major
+  bool identity = false;   // a PHASE of exactly 1: nothing to do
+};
+
+// Validate a gate and reduce it to its cheapest form: controls hidden in
+// the matrix are extracted, then diagonal / X-like / SWAP / dense.
+// Returns a QGB status; on success fills ``op``.
+int qgb_classify(int nqubits, const int* qubits, int k, const int* controls, int ncontrols,
+                 const double* matrix, GateOp* op, const char* fn);
