@@ -108,7 +108,6 @@ typedef struct qgb_op {
 #define QGB_PLAN_BLOCKED 1
 int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, int flags, void* stream);
-
 /* ---- measurement: Backend.calculate_probabilities (:2734-2758,
  *      _order_probabilities :3371-3381), sample_shots / sample_frequencies
  *      (:2760-2801) --------------------------------------------------------- */
@@ -131,6 +130,20 @@ int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scra
 size_t qgb_sample_scratch_bytes(int m);
 int qgb_sample(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
                int64_t* counts, void* scratch, void* stream);
+/* qgb_sample without a scratch argument and without allocating: this entry
+ * point has no counterpart in the reference.  It is for callers that cannot
+ * allocate device memory when they need shots (a state that fills the GPU
+ * leaves no room for a CDF buffer; a serving loop must not call
+ * cudaMalloc/cudaFree, which can synchronise the device).  The CDF lives in a
+ * fixed array inside the library (131 584 bytes held by every GPU that loads
+ * it, until exit), so m is limited to 20 (2^20 outcomes); larger m returns
+ * QGB_ERR_INVALID.  Same outputs as qgb_sample for the same arguments.  The
+ * first call on a device looks up that array's device address (do it before
+ * any stream capture).  All calls share the one array: calls that can overlap
+ * on the GPU (different streams without ordering) race and must not be
+ * issued. */
+int qgb_sample_noalloc(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
+                       int64_t* counts, void* stream);
 /* Raw Philox4x32-10 words: out[4t+e] = word e of philox(counter = (t_lo,
  * t_hi, c2, c3), key = (k0, k1)), t < n4 (device buffer).  Exposes the
  * generator behind qgb_sample for known-answer tests. */

@@ -52,14 +52,14 @@ SIGNATURES = {
     "qgb_apply_2q": (i32, [vp, i32, i32, i32, i32, dp, vp]),
     "qgb_apply_phase": (i32, [vp, i32, i32, ip, i32, f64, f64, vp]),
     "qgb_apply_swap": (i32, [vp, i32, i32, i32, i32, ip, i32, vp]),
-    "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),
-    "qgb_probs_scratch_bytes": (sz, [i32, i32]),
+    "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),    "qgb_probs_scratch_bytes": (sz, [i32, i32]),
     "qgb_probabilities": (i32, [vp, i32, i32, ip, i32, vp, vp, vp]),
     "qgb_norm_scratch_bytes": (sz, []),
     "qgb_norm2": (i32, [vp, i32, i32, vp, vp, vp]),
     "qgb_sample_scratch_bytes": (sz, [i32]),
     "qgb_sample": (i32, [vp, i32, i64, u64, vp, vp, vp, vp]),
     "qgb_philox_fill": (i32, [vp, i64, u32, u32, u32, u32, vp]),
+    "qgb_sample_noalloc": (i32, [vp, i32, i64, u64, vp, vp, vp]),
     "qgb_expect_scratch_bytes": (sz, [i32, i32]),
     "qgb_expect_pauli": (i32, [vp, i32, i32, u64p, u64p, dp, i32, vp, vp, vp]),
     "qgb_expect_dense": (i32, [vp, i32, i32, vp, vp, vp, vp]),

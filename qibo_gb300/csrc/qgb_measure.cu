@@ -16,6 +16,7 @@
 //    that share it, instead of one einsum pass per term.
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "qgb_common.cuh"
@@ -678,3 +679,62 @@ int qgb_expect_pauli(const void* state, int nqubits, int dtype, const uint64_t* 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ sampling without allocation --
+// Some callers cannot allocate device memory at the moment they need shots:
+// a state vector sized to fill the GPU (33-34 qubits) leaves no room for a
+// CDF buffer, and a serving loop that must not stall other requests cannot
+// afford cudaMalloc/cudaFree, which may synchronise the whole device.  For
+// them qgb_sample_noalloc keeps the CDF in a fixed device array that is part
+// of this library's module: every GPU that loads the library holds it
+// (QGB_NOALLOC_SAMPLE_MAX_M = 20, i.e. distributions of up to 2^20 outcomes,
+// 2^14 chunk sums + 64 scan totals = 131 584 bytes) until the process exits.
+#define QGB_NOALLOC_SAMPLE_MAX_M 20
+#define QGB_NOALLOC_SAMPLE_DOUBLES ((1 << (QGB_NOALLOC_SAMPLE_MAX_M - 6)) + 64)
+
+static __device__ __align__(256) double g_noalloc_sample_scratch[QGB_NOALLOC_SAMPLE_DOUBLES];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[64] = {};
+
+// Device address of the built-in scratch for the current device, looked up
+// once per device (host code must not use the array's name as an address).
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  QGB_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    qgb_set_error("qgb_sample_noalloc: device %d beyond the 64 devices supported", dev);
+    return QGB_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sample_scratch);
+    if (e != cudaSuccess) return qgb_cuda_status(e, "cudaGetSymbolAddress(g_noalloc_sample_scratch)");
+    g_noalloc_addr[dev] = (double*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return QGB_OK;
+}
+}  // namespace
+
+extern "C" int qgb_sample_noalloc(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
+                                  int64_t* counts, void* stream) {
+  if (m > QGB_NOALLOC_SAMPLE_MAX_M) {
+    qgb_set_error("qgb_sample_noalloc: a distribution of 2^%d outcomes exceeds the built-in scratch "
+                  "(at most 2^%d outcomes); use qgb_sample with a caller-provided scratch buffer",
+                  m, QGB_NOALLOC_SAMPLE_MAX_M);
+    return QGB_ERR_INVALID;
+  }
+  if (!probs || m < 0 || nshots < 0 || (!samples && !counts)) {
+    qgb_set_error("qgb_sample_noalloc: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  double* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
+  if (st) return st;
+  // Every scratch word the sampler reads (chunk sums, scan totals) is written
+  // earlier in the same call, so nothing has to be cleared between calls.
+  return qgb_sample(probs, m, nshots, seed, samples, counts, scratch, stream);
+}
