@@ -97,7 +97,11 @@ int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1,
  * ``ops`` is an array of ``nops`` qgb_op records, ``coefs`` holds their
  * matrices (each op's ``coef_offset`` indexes doubles).  The engine plans
  * shared-memory passes that apply many gates per read+write of the state
- * when ``flags & QGB_PLAN_BLOCKED``, otherwise it runs gate by gate. */
+ * when ``flags & QGB_PLAN_BLOCKED``, otherwise it runs gate by gate.
+ * Complex128 passes compute in double-float (two FP32 words per double,
+ * about 48 significant bits) on the FP32 pipe unless
+ * ``flags & QGB_PLAN_STRICT_FP64`` asks for IEEE FP64 arithmetic; the
+ * gate-by-gate path always computes complex128 in IEEE FP64. */
 typedef struct qgb_op {
     int32_t k;              /* number of gate qubits (<= 5) */
     int32_t ncontrols;      /* number of controls (<= 8) */
@@ -106,8 +110,13 @@ typedef struct qgb_op {
     int64_t coef_offset;    /* offset (in doubles) of the 2*4^k matrix in coefs */
 } qgb_op;
 #define QGB_PLAN_BLOCKED 1
+#define QGB_PLAN_STRICT_FP64 2
 int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, int flags, void* stream);
+/* Number of state passes QGB_PLAN_BLOCKED would launch for this gate list
+ * (host only, no device work). */
+int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs, int* npasses);
+
 /* ---- measurement: Backend.calculate_probabilities (:2734-2758,
  *      _order_probabilities :3371-3381), sample_shots / sample_frequencies
  *      (:2760-2801) --------------------------------------------------------- */
@@ -167,6 +176,30 @@ size_t qgb_expect_scratch_bytes(int nqubits, int nterms);
  * qgb_expect_scratch_bytes(nqubits, 1) bytes. */
 int qgb_expect_dense(const void* state, int nqubits, int dtype, const double* hamiltonian, double* out,
                      void* scratch, void* stream);
+
+/* ---- gradients: the reference has parameter shift and finite differences
+ *      only (derivative.py:7-226); these implement the adjoint method ----- */
+/* dst = sum_t coef[t] P_t src for Pauli strings given as qubit bit masks
+ * (as qgb_expect_pauli); src and dst are distinct states of the same n.
+ * At most 256 terms in at most 64 distinct X/Y patterns. */
+int qgb_apply_pauli_sum(const void* src, void* dst, int nqubits, int dtype, const uint64_t* xmask,
+                        const uint64_t* zmask, const double* coef, int nterms, void* stream);
+/* out[0..2) (device, FP64) = <a|b> (real, imaginary); scratch of
+ * qgb_inner_scratch_bytes() bytes. */
+size_t qgb_inner_scratch_bytes(void);
+int qgb_inner(const void* a, const void* b, int nqubits, int dtype, double* out, void* scratch, void* stream);
+/* Reverse sweep of the adjoint method.  On entry psi = U_L...U_1 psi_0 and
+ * lam = H psi; ``ops`` lists U_L^dagger, ..., U_1^dagger (matrices in
+ * ``coefs`` as for qgb_apply_circuit).  For op i with nder[i] > 0 (at most 3,
+ * gates on at most 2 qubits), coefs + der_offset[i] holds nder[i] matrices
+ * dU/dtheta (of U, not of U^dagger) and the derivatives are written to
+ * grads[grad_index[i] + j] (device, FP64): dE/dtheta = 2 Re <lam|dU psi>.
+ * Each parameter slot belongs to one op.  On return psi = psi_0.  Scratch:
+ * qgb_adjoint_scratch_bytes(nparams) bytes. */
+size_t qgb_adjoint_scratch_bytes(int nparams);
+int qgb_adjoint_sweep(void* psi, void* lam, int nqubits, int dtype, const qgb_op* ops, int nops,
+                      const double* coefs, const int* nder, const int64_t* der_offset, const int* grad_index,
+                      int nparams, double* grads, void* scratch, void* stream);
 
 /* ---- timing helpers (events on the caller's stream) ------------------- */
 int qgb_event_create(void** ev);

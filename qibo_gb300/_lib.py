@@ -15,6 +15,7 @@ from . import _build
 QGB_OK, QGB_ERR_INVALID, QGB_ERR_OOM, QGB_ERR_CUDA, QGB_ERR_TIMEOUT, QGB_ERR_UNSUPPORTED = range(6)
 QGB_C64, QGB_C128 = 0, 1
 QGB_PLAN_BLOCKED = 1
+QGB_PLAN_STRICT_FP64 = 2
 
 vp, i32, i64, u32, u64, f64, sz = C.c_void_p, C.c_int, C.c_int64, C.c_uint32, C.c_uint64, C.c_double, C.c_size_t
 ip = C.POINTER(C.c_int)
@@ -52,7 +53,9 @@ SIGNATURES = {
     "qgb_apply_2q": (i32, [vp, i32, i32, i32, i32, dp, vp]),
     "qgb_apply_phase": (i32, [vp, i32, i32, ip, i32, f64, f64, vp]),
     "qgb_apply_swap": (i32, [vp, i32, i32, i32, i32, ip, i32, vp]),
-    "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),    "qgb_probs_scratch_bytes": (sz, [i32, i32]),
+    "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),
+    "qgb_plan_passes": (i32, [i32, i32, C.POINTER(QgbOp), i32, dp, ip]),
+    "qgb_probs_scratch_bytes": (sz, [i32, i32]),
     "qgb_probabilities": (i32, [vp, i32, i32, ip, i32, vp, vp, vp]),
     "qgb_norm_scratch_bytes": (sz, []),
     "qgb_norm2": (i32, [vp, i32, i32, vp, vp, vp]),
@@ -63,6 +66,12 @@ SIGNATURES = {
     "qgb_expect_scratch_bytes": (sz, [i32, i32]),
     "qgb_expect_pauli": (i32, [vp, i32, i32, u64p, u64p, dp, i32, vp, vp, vp]),
     "qgb_expect_dense": (i32, [vp, i32, i32, vp, vp, vp, vp]),
+    "qgb_apply_pauli_sum": (i32, [vp, vp, i32, i32, u64p, u64p, dp, i32, vp]),
+    "qgb_inner_scratch_bytes": (sz, []),
+    "qgb_inner": (i32, [vp, vp, i32, i32, vp, vp, vp]),
+    "qgb_adjoint_scratch_bytes": (sz, [i32]),
+    "qgb_adjoint_sweep": (i32, [vp, vp, i32, i32, C.POINTER(QgbOp), i32, dp, ip, C.POINTER(C.c_int64), ip, i32,
+                                vp, vp, vp]),
     "qgb_event_create": (i32, [C.POINTER(vp)]),
     "qgb_event_destroy": (i32, [vp]),
     "qgb_event_record": (i32, [vp, vp]),

@@ -72,7 +72,10 @@ class GB300Methods:
         self.oom_error = DeviceOutOfMemory
         self._seed = None
         self._seed_calls = 0
+        # shared-memory multi-gate passes (QIBO_GB300_BLOCKED=0: one kernel per gate)
         self.blocked = os.environ.get("QIBO_GB300_BLOCKED", "1") != "0"
+        # complex128 passes in IEEE FP64 instead of double-float (QIBO_GB300_STRICT_FP64=1)
+        self.strict_fp64 = os.environ.get("QIBO_GB300_STRICT_FP64", "0") == "1"
 
     # -- states -----------------------------------------------------------
     def zero_state(self, nqubits, density_matrix=False, dtype=None):
@@ -141,7 +144,7 @@ class GB300Methods:
                     dt = arr.dtype if arr.dtype in (np.complex64, np.complex128) else self.dtype
                     state = DeviceState.from_numpy(arr, dt)
             descs = [d for d in (describe_gate(g, self) for g in circuit.queue) if d is not None]
-            self.engine_gb.apply_many(state, descs, blocked=self.blocked)
+            self.engine_gb.apply_many(state, descs, blocked=self.blocked, strict_fp64=self.strict_fp64)
         except DeviceOutOfMemory:
             raise RuntimeError(f"State does not fit in {self.device} memory."
                                "Please switch the execution device to a "

@@ -530,7 +530,7 @@ int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1, const in
 // ---------------------------------------------------------------------------
 // whole circuits
 int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
-                    cudaStream_t s);  // qgb_blocked.cu
+                    bool strict_fp64, cudaStream_t s);  // qgb_blocked.cu
 
 extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                                  const double* coefs, int flags, void* stream) {
@@ -538,7 +538,8 @@ extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_
   int st = check_state_args(state, dtype, "qgb_apply_circuit");
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  if (flags & QGB_PLAN_BLOCKED) return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, s);
+  if (flags & QGB_PLAN_BLOCKED)
+    return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0, s);
   for (int i = 0; i < nops; ++i) {
     const qgb_op& op = ops[i];
     GateOp g;

@@ -42,11 +42,35 @@ class Engine:
                                       int_array(controls), len(controls),
                                       m.ctypes.data_as(_lib.dp), self.rt.stream))
 
-    def apply_many(self, state: DeviceState, descs: Iterable[GateDesc], blocked: bool = False):
-        """Apply a gate list with one C call (``qgb_apply_circuit``)."""
+    def apply_many(self, state: DeviceState, descs: Iterable[GateDesc], blocked: bool = False,
+                   strict_fp64: bool = False):
+        """Apply a gate list with one C call (``qgb_apply_circuit``).
+
+        ``blocked`` plans shared-memory passes (many gates per read+write of
+        the state); complex128 passes then compute in double-float unless
+        ``strict_fp64``."""
         descs = list(descs)
         if not descs:
             return
+        ops, allc = self.pack_ops(descs)
+        flags = (_lib.QGB_PLAN_BLOCKED if blocked else 0) | (_lib.QGB_PLAN_STRICT_FP64 if strict_fp64 else 0)
+        check(self.lib.qgb_apply_circuit(state.ptr, state.nqubits, state.code, ops, len(descs),
+                                         allc.ctypes.data_as(_lib.dp), flags, self.rt.stream))
+
+    def count_passes(self, nqubits: int, dtype_code: int, descs: Iterable[GateDesc]) -> int:
+        """State passes the shared-memory planner makes for this gate list."""
+        descs = list(descs)
+        if not descs:
+            return 0
+        ops, allc = self.pack_ops(descs)
+        n = C.c_int(0)
+        check(self.lib.qgb_plan_passes(nqubits, dtype_code, ops, len(descs), allc.ctypes.data_as(_lib.dp),
+                                       C.byref(n)))
+        return n.value
+
+    @staticmethod
+    def pack_ops(descs: List[GateDesc]):
+        """``qgb_op`` records plus the concatenated matrix coefficients."""
         ops = (QgbOp * len(descs))()
         coefs: List[np.ndarray] = []
         off = 0
@@ -67,10 +91,7 @@ class Engine:
             op.coef_offset = off
             coefs.append(m)
             off += m.size
-        allc = np.concatenate(coefs)
-        check(self.lib.qgb_apply_circuit(state.ptr, state.nqubits, state.code, ops, len(descs),
-                                         allc.ctypes.data_as(_lib.dp),
-                                         _lib.QGB_PLAN_BLOCKED if blocked else 0, self.rt.stream))
+        return ops, np.concatenate(coefs)
 
     # -- reductions -------------------------------------------------------
     def probabilities(self, state: DeviceState, qubits: Sequence[int]) -> DeviceArray:

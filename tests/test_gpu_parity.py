@@ -49,16 +49,18 @@ def make_circuit(n, ops):
     return c
 
 
-def run(backend, n, ops, psi=None, dtype="complex128", blocked=None):
+def run(backend, n, ops, psi=None, dtype="complex128", blocked=None, strict=False):
     backend.set_dtype(dtype)
     if blocked is not None:
         backend.blocked = blocked
+    backend.strict_fp64 = strict
     try:
         res = backend.execute_circuit(make_circuit(n, ops), None if psi is None else psi.copy())
         return np.asarray(res.state())
     finally:
         backend.set_dtype("complex128")
         backend.blocked = True
+        backend.strict_fp64 = False
 
 
 def rand_state(n, seed, dtype=np.complex128):
@@ -116,9 +118,26 @@ def test_every_position_every_kind(backend, n):
         ops.append(("U3", (int(c),), (0.3, 0.2, 0.1), (int(a), int(b))))
     psi = rand_state(n, 100 + n)
     want = ref.execute(ops, n, psi)
+    # per-gate kernels (IEEE FP64), shared-memory passes in double-float, and
+    # shared-memory passes in IEEE FP64
+    for blocked, strict in ((False, False), (True, False), (True, True)):
+        got = run(backend, n, ops, psi, blocked=blocked, strict=strict)
+        assert np.max(np.abs(got - want)) < TOL128, (blocked, strict)
+    want64 = ref.execute(ops, n, psi.astype(np.complex64), dtype="complex64")
     for blocked in (False, True):
-        got = run(backend, n, ops, psi, blocked=blocked)
-        assert np.max(np.abs(got - want)) < TOL128, blocked
+        got = run(backend, n, ops, psi.astype(np.complex64), dtype="complex64", blocked=blocked)
+        assert np.max(np.abs(got - want64)) < TOL64 * 10, blocked
+
+
+@pytest.mark.parametrize("n", [16, 20])
+def test_deep_random_circuit_c128_passes(backend, n):
+    """890-gate-scale accuracy of the double-float passes: a depth-30 U3+CZ
+    brickwork plus QFT against the FP64 oracle."""
+    ops = ref.brickwork_ops(n, 30, 5) + ref.qft_ops(n)
+    psi = rand_state(n, 77)
+    want = ref.execute(ops, n, psi)
+    got = run(backend, n, ops, psi, blocked=True)
+    assert np.max(np.abs(got - want)) < TOL128
 
 
 def test_unitary_gates_up_to_5_qubits(backend):
