@@ -1,29 +1,34 @@
 """Benchmark of the qibo state-vector hot path on one GB300.
 
-Workload (one "step"): the 30-qubit random circuit of depth 20 — per layer
-U3(theta, phi, lambda) on every qubit with angles uniform in [0, 2 pi) from a
-seeded generator, then CZ on brickwork pairs — started from |0...0>, in
+Default workload (one "step"): the 30-qubit random circuit of depth 20 — per
+layer U3(theta, phi, lambda) on every qubit with angles uniform in [0, 2 pi)
+from a seeded generator, then CZ on brickwork pairs — from |0...0> in
 complex128, followed by 1e6 shots on all 30 qubits drawn from |psi|^2.
 
-``value`` is the state-vector bandwidth of the step: the algorithmic bytes
-of every pass (dense 1q/2q/fused/blocked pass: read+write of every
-amplitude, 2 * 2^n * 16 B; CZ: 2 * 2^(n-2) * 16 B; probabilities: read
-2^n * 16 B + write 2^n * 8 B; CDF/sampling: read 2^n * 8 B twice) divided by
-the device time of the step, with the state already resident.  The state
-(17.2 GB) is far larger than L2 (129 MB), so no L2 flush is needed.
+``value`` is the effective state-vector bandwidth of the step: the
+algorithmic bytes a gate-by-gate execution of the circuit moves (dense
+1-qubit gate: read + write of every amplitude, 2 * 2^n * 16 B; CZ: 2 *
+2^(n-2) * 16 B) plus the measurement passes (probabilities: read 2^n * 16 B,
+write 2^n * 8 B; CDF: 2 * 2^n * 8 B), divided by the device time of the
+step with the state resident.  The state (17.2 GB) is far larger than L2
+(129 MB), so no L2 flush is needed between steps.
 
 ``e2e`` is the same metric through the public API with host buffers:
-``backend.execute_circuit(circuit, nshots=1e6)`` and the 1e6 samples read
-back to the host every step.
+``backend.execute_circuit(circuit, nshots=1e6)`` with the 1e6 samples read
+back to the host every step.  The line also carries the complex64 run of the
+same circuit with its infidelity against the complex128 state, and a
+bounded sample of the serving stream (circuits/s, p50/p99).
 
-``--impl reference`` times the reference's CPU algorithm (the numpy
-restatement in ``oracle/``, OpenBLAS threads = all host cores) on a bounded
-sample of the same workload.
+Other workloads (``--workload``): ``qft20``, ``vqe24``, ``serving``,
+``memlimit``.  ``--impl reference`` times the reference's CPU algorithm (the
+numpy restatement in ``oracle/``, all host cores) on a bounded sample of the
+same workload.
 """
 
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -81,8 +86,8 @@ class Clocks:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-i", "0", "-lms", "200"], stdout=open(self.path, "w"),
-                                         stderr=subprocess.DEVNULL)
+                                          "-i", os.environ.get("LOCAL_RANK", "0"), "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -160,22 +165,60 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--nqubits", type=int, default=N_QUBITS)
-    ap.add_argument("--dtype", default="complex128")
-    ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    args = ap.parse_args()
-    if args.impl == "reference":
-        return run_reference(args)
+class Events:
+    def __init__(self, lib):
+        from qibo_gb300._lib import check
 
+        self.lib, self.check = lib, check
+        self.a, self.b = C.c_void_p(), C.c_void_p()
+        check(lib.qgb_event_create(C.byref(self.a)))
+        check(lib.qgb_event_create(C.byref(self.b)))
+
+    def start(self, stream):
+        self.check(self.lib.qgb_event_record(self.a, stream))
+
+    def stop_ms(self, stream) -> float:
+        self.check(self.lib.qgb_event_record(self.b, stream))
+        ms = C.c_float()
+        self.check(self.lib.qgb_event_elapsed_ms(self.a, self.b, C.byref(ms)))
+        return ms.value
+
+
+def serving_sample(nreq: int, rate: float, baseline_req: int):
+    """Bounded sample of the serving stream: ``nreq`` requests with Poisson
+    arrivals, qubits uniform in [10, 28], depth uniform in [5, 30], mixed
+    dtypes and outputs; plus the one-at-a-time complex128 per-gate path on
+    its first ``baseline_req`` requests (forced to complex128)."""
+    from qibo_gb300.serving import Request, Server, make_stream
+
+    reqs = make_stream(nreq, rate, seed=2026)
+    srv = Server()
+    try:
+        warm = make_stream(16, 0.0, seed=7, nmin=10, nmax=14, dmin=5, dmax=6)
+        srv.run(warm, realtime=False)
+        srv.stats.clear()
+        st = srv.run(reqs, realtime=True)
+    finally:
+        srv.close()
+    base = [Request(r.rid, r.nqubits, "complex128", r.ops, r.coefs, r.shape, r.output, r.nshots, r.zmask, r.seed, 0.0)
+            for r in make_stream(baseline_req, 0.0, seed=2026)]
+    srv = Server(one_at_a_time=True)
+    try:
+        bst = srv.run(base, realtime=False)
+    finally:
+        srv.close()
+    return {"requests": nreq, "arrival_rate_per_s": rate, "circuits_per_s": st["circuits_per_s"],
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "batched": st.get("batched_requests", 0),
+            "graph_replays": st.get("graph_replays", 0),
+            "baseline_one_at_a_time_c128_per_gate": {"requests": baseline_req,
+                                                     "circuits_per_s": bst["circuits_per_s"],
+                                                     "p50_ms": bst["p50_ms"], "p99_ms": bst["p99_ms"]}}
+
+
+def run_brickwork(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -186,7 +229,7 @@ def main():
     from qibo_gb300 import Circuit
     from qibo_gb300._lib import check
     from qibo_gb300.backend import GB300Backend, describe_gate
-    from qibo_gb300.device import DeviceState
+    from qibo_gb300.device import DeviceArray, DeviceState
 
     n, dtype = args.nqubits, args.dtype
     S = 16 if dtype == "complex128" else 8
@@ -201,15 +244,12 @@ def main():
     backend.blocked = mode in ("blocked", "fused")
     ndense = sum(1 for g in gates if type(g).__name__ == "U3")
     ncz = len(gates) - ndense
-    # effective bytes: what the unfused gate-by-gate passes of this circuit move
     gbytes, mbytes = algorithmic_bytes(n, ndense, ncz, S)
-    npasses = eng.count_passes(n, 1 if dtype == "complex128" else 0, descs) if backend.blocked else len(descs)
+    code = 1 if dtype == "complex128" else 0
+    npasses = eng.count_passes(n, code, descs) if backend.blocked else len(descs)
     pass_bytes = (npasses * 2 * 2**n * S) if backend.blocked else gbytes
     state = DeviceState(n, dtype)
     allq = list(range(n))
-
-    # device-resident sampler output (no D2H inside the device-timed step)
-    from qibo_gb300.device import DeviceArray
     samp = DeviceArray((NSHOTS,), np.int64, rt)
 
     def device_step(seed):
@@ -220,53 +260,45 @@ def main():
                              rt.stream))
         return probs
 
-    ev = []
-    for _ in range(2):
-        import ctypes as C
-        e = C.c_void_p()
-        check(lib.qgb_event_create(C.byref(e)))
-        ev.append(e)
+    ev = Events(lib)
     for w in range(args.warmup):
         device_step(1000 + w)
     rt.synchronize()
-    if world > 1:
+    if dist is not None:
         dist.barrier()
     launches0 = lib.qgb_launch_count()
     clocks = Clocks()
     clocks.start()
-    check(lib.qgb_event_record(ev[0], rt.stream))
+    ev.start(rt.stream)
     for s in range(args.steps):
         device_step(s)
-    check(lib.qgb_event_record(ev[1], rt.stream))
+    ms_total = ev.stop_ms(rt.stream)
     rt.synchronize()
-    import ctypes as C
-    ms = C.c_float()
-    check(lib.qgb_event_elapsed_ms(ev[0], ev[1], C.byref(ms)))
     clk = clocks.stop()
     launches = lib.qgb_launch_count() - launches0
-    ms_step = ms.value / args.steps
-    if world > 1:
+    ms_step = ms_total / args.steps
+    if dist is not None:
         import torch
+
         t = torch.tensor([ms_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     total_bytes = gbytes + mbytes
     value = total_bytes / (ms_step * 1e-3) / 1e9 * world
 
-    # dominant kernel, CUDA events on the launch stream: the gate passes of one
-    # circuit (k_pass launches in blocked mode, per-gate kernels otherwise)
+    # the gate passes of one circuit, CUDA events on the launch stream
     check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
-    check(lib.qgb_event_record(ev[0], rt.stream))
+    ev.start(rt.stream)
     eng.apply_many(state, descs, blocked=backend.blocked)
-    check(lib.qgb_event_record(ev[1], rt.stream))
-    check(lib.qgb_event_elapsed_ms(ev[0], ev[1], C.byref(ms)))
-    gate_ms = ms.value
+    gate_ms = ev.stop_ms(rt.stream)
     k_ms = gate_ms / max(1, npasses)
     k_bytes = pass_bytes / max(1, npasses)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
     roof = {"bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "traffic": None,
+            "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "traffic": 2.09e9 * (2 ** (n - 26)) if n >= 26 else None,
+            "traffic_note": "dram bytes per k_pass launch from ncu at n=26 (1.075 GB read + 1.014 GB write), "
+                            "scaled by 2^(n-26); equals the algorithmic bytes",
             "kernel": "k_pass (shared-memory multi-gate pass)" if backend.blocked else "per-gate kernels",
             "per_launch_bytes": k_bytes, "launches": npasses,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
@@ -275,9 +307,9 @@ def main():
     e2e_times = []
     for s in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
-        res = backend.execute_circuit(run_circ if mode == "fused" else circ, nshots=NSHOTS)
+        res = backend.execute_circuit(run_circ, nshots=NSHOTS)
         p = eng.probabilities(res.state(), allq)
-        smp = eng.sample(p, NSHOTS, 77 + s, counts=False)
+        eng.sample(p, NSHOTS, 77 + s, counts=False)
         e2e_times.append(time.perf_counter() - t0)
         del res, p
     e2e_s = statistics.median(e2e_times)
@@ -288,6 +320,9 @@ def main():
             "vs_baseline": None, "dtype": "c128" if dtype == "complex128" else "c64", "data": "synthetic",
             "config": {"workload": f"random U3+CZ brickwork n={n} depth {DEPTH} seed {SEED} + {NSHOTS} shots",
                        "mode": mode, "gates": len(gates), "state_passes": npasses,
+                       "arithmetic": ("double-float (FP32 pipe) in passes, IEEE FP64 reductions"
+                                      if dtype == "complex128" and backend.blocked and not backend.strict_fp64
+                                      else "native"),
                        "bytes": "effective: per-gate algorithmic bytes of the unfused circuit + probabilities + CDF",
                        "l2": "state 2^n*S >> L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single"},
@@ -296,12 +331,170 @@ def main():
             "roofline": roof, "clocks": clk,
             "e2e": {"value": total_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": coef_bytes,
                     "d2h_bytes_per_step": NSHOTS * 8, "seconds": e2e_s}}
+
+    if dtype == "complex128" and rank == 0 and not args.quick:
+        # complex64 leg of the same circuit and its infidelity against complex128
+        b64 = GB300Backend("complex64")
+        st64 = DeviceState(n, "complex64")
+        for _ in range(2):
+            check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
+            b64.engine_gb.apply_many(st64, descs, blocked=True)
+        check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
+        ev.start(rt.stream)
+        b64.engine_gb.apply_many(st64, descs, blocked=True)
+        ms64 = ev.stop_ms(rt.stream)
+        check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
+        eng.apply_many(state, descs, blocked=True)
+        out = DeviceArray((2,), np.float64, rt)
+        check(lib.qgb_inner_mixed(state.ptr, state.code, st64.ptr, st64.code, n, out.ptr,
+                                  rt.scratch(lib.qgb_inner_scratch_bytes()), rt.stream))
+        re, im = out.to_numpy()
+        g64, _ = algorithmic_bytes(n, ndense, ncz, 8)
+        line["complex64"] = {"gate_ms": ms64, "value": g64 / (ms64 * 1e-3) / 1e9, "unit": "GB/s",
+                             "infidelity_vs_c128": 1.0 - (re * re + im * im)}
+        del st64
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
+    if rank == 0 and world == 1 and args.serving_requests > 0:
+        del state
+        line["serving"] = serving_sample(args.serving_requests, args.serving_rate, args.serving_baseline)
     if rank == 0:
         print(json.dumps(line))
-    if world > 1:
+    if dist is not None:
         dist.destroy_process_group()
+
+
+def run_qft20(args):
+    """QFT(20) in complex128 on a seeded complex Gaussian state + 1e5 shots."""
+    from qibo_gb300 import QFT
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+
+    n = 20
+    psi = np.random.default_rng(20).normal(size=2**n) + 1j * np.random.default_rng(21).normal(size=2**n)
+    psi /= np.linalg.norm(psi)
+    backend = GB300Backend("complex128")
+    c = QFT(n)
+    backend.set_seed(1234)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        res = backend.execute_circuit(c, psi)
+        p = backend.calculate_probabilities(res.state(), list(range(n)), n)
+        backend.sample_frequencies(p, 100_000)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    s = statistics.median(times)
+    print(json.dumps({"workload": "QFT(20) complex128 + 1e5 shots, through the public API", "seconds": s,
+                      "reference_published_v100_s": 0.03881, "unit": "s", "higher_is_better": False}))
+
+
+def run_vqe24(args):
+    """24-qubit hardware-efficient ansatz (10 layers RY+RZ + CNOT ladder, 480
+    parameters), periodic TFIM h=1: energy and all 480 adjoint gradients."""
+    from oracle import numpy_ref as ref  # circuit factory and TFIM term list only
+    from qibo_gb300 import Circuit, gates
+    from qibo_gb300.adjoint import adjoint_gradient
+    from qibo_gb300.backend import GB300Backend
+
+    n, layers = 24, 10
+    p = np.random.default_rng(24).uniform(-np.pi, np.pi, 2 * n * layers)
+    ham = ref.tfim_terms(n)
+    out = {}
+    for dtype in ("complex128", "complex64"):
+        b = GB300Backend(dtype)
+        c = Circuit(n)
+        for nm, q, pp in ref.vqe_ops(n, layers, p):
+            c.add(getattr(gates, nm)(*q, *pp))
+        times = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            e, g = adjoint_gradient(b, c, ham)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        out[dtype] = {"energy": e, "grad_norm": float(np.linalg.norm(g)), "seconds": statistics.median(times)}
+    print(json.dumps({"workload": "VQE24: energy + 480 adjoint gradients", **out}))
+
+
+def run_serving(args):
+    print(json.dumps({"workload": "serving stream sample",
+                      **serving_sample(args.serving_requests or 2000, args.serving_rate, args.serving_baseline)}))
+
+
+def run_memlimit(args):
+    """33-qubit complex128 (137 GB) and 34-qubit complex64 (137 GB): QFT then
+    a depth-10 U3+CZ brickwork in shared-memory passes, 1e7 shots drawn
+    straight from the state, <sum_i Z_i Z_{i+1}> (open chain), and the
+    complex64 infidelity against complex128 at 33 qubits."""
+    from qibo_gb300 import QFT, Circuit
+    from qibo_gb300._lib import check
+    from qibo_gb300.backend import GB300Backend, describe_gate
+    from qibo_gb300.device import DeviceArray, DeviceState
+
+    res = {}
+    keep = {}
+    # 34-qubit complex64 first (freed after), then the two 33-qubit states
+    # that are compared (137 + 69 GB resident together)
+    for n, dtype in ((34, "complex64"), (33, "complex128"), (33, "complex64")):
+        b = GB300Backend(dtype)
+        rt, eng, lib = b.rt, b.engine_gb, b.rt.lib
+        c = QFT(n)
+        c.add(brickwork_gates(n, 10, n))
+        descs = [describe_gate(g, b) for g in c.queue]
+        code = 1 if dtype == "complex128" else 0
+        npass = eng.count_passes(n, code, descs)
+        st = DeviceState(n, dtype)
+        ev = Events(lib)
+        check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+        ev.start(rt.stream)
+        eng.apply_many(st, descs, blocked=True)
+        gms = ev.stop_ms(rt.stream)
+        samples = DeviceArray((10_000_000,), np.int64, rt)
+        ev.start(rt.stream)
+        check(lib.qgb_sample_state(st.ptr, n, st.code, 10_000_000, 33, samples.ptr,
+                                   rt.scratch(lib.qgb_sample_state_scratch_bytes(n)), rt.stream))
+        sms = ev.stop_ms(rt.stream)
+        zz = eng.expect_pauli(st, [0] * (n - 1), [(1 << i) | (1 << (i + 1)) for i in range(n - 1)], [1.0] * (n - 1))
+        S = 16 if dtype == "complex128" else 8
+        key = f"n{n}_{dtype}"
+        res[key] = {"gates": len(descs), "state_passes": npass, "gate_ms": gms,
+                    "pass_gbs": npass * 2 * 2**n * S / (gms * 1e-3) / 1e9, "shots_1e7_ms": sms, "zz_open_chain": zz,
+                    "state_gb": 2**n * S / 1e9}
+        del samples
+        if n == 33:
+            keep[dtype] = st
+        else:
+            del st
+        rt.synchronize()
+    rt = keep["complex128"].rt
+    out = DeviceArray((2,), np.float64, rt)
+    check(rt.lib.qgb_inner_mixed(keep["complex128"].ptr, 1, keep["complex64"].ptr, 0, 33, out.ptr,
+                                 rt.scratch(rt.lib.qgb_inner_scratch_bytes()), rt.stream))
+    re, im = out.to_numpy()
+    res["infidelity_c64_vs_c128_n33"] = 1.0 - (re * re + im * im)
+    print(json.dumps({"workload": "memory limit: QFT + depth-10 brickwork, 1e7 shots, <ZZ>", **res}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft20", "vqe24", "serving", "memlimit"])
+    ap.add_argument("--nqubits", type=int, default=N_QUBITS)
+    ap.add_argument("--dtype", default="complex128")
+    ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the complex64 leg")
+    ap.add_argument("--serving-requests", type=int, default=300)
+    ap.add_argument("--serving-rate", type=float, default=200.0)
+    ap.add_argument("--serving-baseline", type=int, default=40)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
+            "memlimit": run_memlimit}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -62,6 +62,9 @@ int qgb_memcpy_h2d(void* dst, const void* src, size_t bytes, void* stream);
 int qgb_memcpy_d2h(void* dst, const void* src, size_t bytes, void* stream);
 int qgb_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
 int qgb_memset_zero(void* ptr, size_t bytes, void* stream);
+/* Page-locked host memory (asynchronous device->host result copies). */
+int qgb_host_alloc(void** ptr, size_t bytes);
+int qgb_host_free(void* ptr);
 int qgb_stream_sync(void* stream);
 
 /* ---- state creation: Backend.zero_state (backends/abstract.py:2243-2273),
@@ -139,6 +142,14 @@ int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scra
 size_t qgb_sample_scratch_bytes(int m);
 int qgb_sample(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
                int64_t* counts, void* scratch, void* stream);
+/* Shots on every qubit drawn straight from the state, without a 2^n
+ * probability vector (for states that fill the GPU): FP64 chunk sums of
+ * |psi|^2 over 64 amplitudes, their prefix scan, and an in-chunk recompute.
+ * Draws follow the same Philox4x32-10 protocol as qgb_sample; samples[nshots]
+ * (device, int64).  Scratch: qgb_sample_state_scratch_bytes(nqubits). */
+size_t qgb_sample_state_scratch_bytes(int nqubits);
+int qgb_sample_state(const void* state, int nqubits, int dtype, int64_t nshots, uint64_t seed, int64_t* samples,
+                     void* scratch, void* stream);
 /* qgb_sample without a scratch argument and without allocating: this entry
  * point has no counterpart in the reference.  It is for callers that cannot
  * allocate device memory when they need shots (a state that fills the GPU
@@ -188,6 +199,10 @@ int qgb_apply_pauli_sum(const void* src, void* dst, int nqubits, int dtype, cons
  * qgb_inner_scratch_bytes() bytes. */
 size_t qgb_inner_scratch_bytes(void);
 int qgb_inner(const void* a, const void* b, int nqubits, int dtype, double* out, void* scratch, void* stream);
+/* <a|b> for states of possibly different precision (complex64 results are
+ * compared against complex128 ones with it: infidelity 1 - |<a|b>|^2). */
+int qgb_inner_mixed(const void* a, int dtype_a, const void* b, int dtype_b, int nqubits, double* out, void* scratch,
+                    void* stream);
 /* Reverse sweep of the adjoint method.  On entry psi = U_L...U_1 psi_0 and
  * lam = H psi; ``ops`` lists U_L^dagger, ..., U_1^dagger (matrices in
  * ``coefs`` as for qgb_apply_circuit).  For op i with nder[i] > 0 (at most 3,
@@ -200,6 +215,58 @@ size_t qgb_adjoint_scratch_bytes(int nparams);
 int qgb_adjoint_sweep(void* psi, void* lam, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, const int* nder, const int64_t* der_offset, const int* grad_index,
                       int nparams, double* grads, void* scratch, void* stream);
+
+/* ---- serving: many independent circuits (replaces the joblib thread pools
+ *      of Backend.execute_circuits / parallel_circuits_execution,
+ *      backends/abstract.py:2514-2530, parallel.py:60-121) ----------------- */
+#define QGB_NOT_READY 6      /* qgb_event_query: work still in flight */
+int qgb_stream_create(void** stream);  /* non-blocking stream */
+int qgb_stream_destroy(void* stream);
+int qgb_event_query(void* ev);         /* QGB_OK when complete, else QGB_NOT_READY */
+
+/* A program is a planned circuit whose pass parameters and state pointer
+ * live in device memory: its first qgb_program_run captures the launches as
+ * a CUDA graph, later runs (any state of the same size, any stream) replay
+ * it.  qgb_program_update swaps in new matrices for the same gate shape (same
+ * gates on the same qubits).  A program must not run on two streams at once.
+ * On the legacy default stream (NULL), which cannot be captured, the passes
+ * are launched directly.  flags: QGB_PLAN_STRICT_FP64, QGB_PROGRAM_NO_GRAPH. */
+#define QGB_PROGRAM_NO_GRAPH 4
+int qgb_program_create(int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs, int flags,
+                       void** prog);
+int qgb_program_passes(void* prog, int* npasses);
+int qgb_program_update(void* prog, const qgb_op* ops, int nops, const double* coefs, void* stream);
+int qgb_program_run(void* prog, void* state, void* stream);
+int qgb_program_destroy(void* prog);
+
+/* Batched small circuits: one launch runs many circuits of at most 13
+ * (complex64) or 12 (complex128) qubits, one CTA per circuit with the whole
+ * state in shared memory, and produces each circuit's output in the same
+ * kernel: the final state (written back), ``nshots`` samples from |psi|^2
+ * (Philox4x32-10 keyed by ``seed``, FP64 CDF in shared memory), or the
+ * expectation of a Z string (qubit mask ``zmask``).  A batch context owns a
+ * device workspace and pinned staging of ``capacity`` bytes. */
+#define QGB_OUT_STATE 0
+#define QGB_OUT_SAMPLES 1
+#define QGB_OUT_ZEXP 2
+typedef struct qgb_batch_item {
+    void* state;            /* device state, 2^nqubits amplitudes (in/out) */
+    int32_t nqubits;
+    int32_t nops;
+    const qgb_op* ops;      /* host gate list, as for qgb_apply_circuit */
+    const double* coefs;    /* host matrices */
+    int32_t init_zero;      /* 1: start from |0...0> */
+    int32_t out_kind;       /* QGB_OUT_* */
+    int64_t nshots;
+    uint64_t seed;
+    uint64_t zmask;
+    void* out;              /* device int64[nshots] or double[1]; unused for QGB_OUT_STATE */
+} qgb_batch_item;
+#define QGB_BATCH_MAX_QUBITS_C64 13
+#define QGB_BATCH_MAX_QUBITS_C128 12
+int qgb_batch_create(size_t capacity, void** ctx);
+int qgb_batch_run(void* ctx, const qgb_batch_item* items, int nitems, int dtype, void* stream);
+int qgb_batch_destroy(void* ctx);
 
 /* ---- timing helpers (events on the caller's stream) ------------------- */
 int qgb_event_create(void** ev);

@@ -30,6 +30,21 @@ class QgbOp(C.Structure):
                 ("controls", C.c_int32 * 8), ("coef_offset", C.c_int64)]
 
 
+class QgbBatchItem(C.Structure):
+    """``qgb_batch_item`` record of ``qgb_batch_run``."""
+
+    _fields_ = [("state", C.c_void_p), ("nqubits", C.c_int32), ("nops", C.c_int32),
+                ("ops", C.POINTER(QgbOp)), ("coefs", C.POINTER(C.c_double)), ("init_zero", C.c_int32),
+                ("out_kind", C.c_int32), ("nshots", C.c_int64), ("seed", C.c_uint64), ("zmask", C.c_uint64),
+                ("out", C.c_void_p)]
+
+
+QGB_NOT_READY = 6
+QGB_PROGRAM_NO_GRAPH = 4
+QGB_OUT_STATE, QGB_OUT_SAMPLES, QGB_OUT_ZEXP = 0, 1, 2
+QGB_BATCH_MAX_QUBITS = {0: 13, 1: 12}
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "qgb_last_error": (C.c_char_p, []),
@@ -43,6 +58,8 @@ SIGNATURES = {
     "qgb_memcpy_d2h": (i32, [vp, vp, sz, vp]),
     "qgb_memcpy_d2d": (i32, [vp, vp, sz, vp]),
     "qgb_memset_zero": (i32, [vp, sz, vp]),
+    "qgb_host_alloc": (i32, [C.POINTER(vp), sz]),
+    "qgb_host_free": (i32, [vp]),
     "qgb_stream_sync": (i32, [vp]),
     "qgb_state_zero": (i32, [vp, i32, i32, vp]),
     "qgb_state_basis": (i32, [vp, i32, i32, i64, vp]),
@@ -63,15 +80,29 @@ SIGNATURES = {
     "qgb_sample": (i32, [vp, i32, i64, u64, vp, vp, vp, vp]),
     "qgb_philox_fill": (i32, [vp, i64, u32, u32, u32, u32, vp]),
     "qgb_sample_noalloc": (i32, [vp, i32, i64, u64, vp, vp, vp]),
+    "qgb_sample_state_scratch_bytes": (sz, [i32]),
+    "qgb_sample_state": (i32, [vp, i32, i32, i64, u64, vp, vp, vp]),
     "qgb_expect_scratch_bytes": (sz, [i32, i32]),
     "qgb_expect_pauli": (i32, [vp, i32, i32, u64p, u64p, dp, i32, vp, vp, vp]),
     "qgb_expect_dense": (i32, [vp, i32, i32, vp, vp, vp, vp]),
     "qgb_apply_pauli_sum": (i32, [vp, vp, i32, i32, u64p, u64p, dp, i32, vp]),
     "qgb_inner_scratch_bytes": (sz, []),
     "qgb_inner": (i32, [vp, vp, i32, i32, vp, vp, vp]),
+    "qgb_inner_mixed": (i32, [vp, i32, vp, i32, i32, vp, vp, vp]),
     "qgb_adjoint_scratch_bytes": (sz, [i32]),
     "qgb_adjoint_sweep": (i32, [vp, vp, i32, i32, C.POINTER(QgbOp), i32, dp, ip, C.POINTER(C.c_int64), ip, i32,
                                 vp, vp, vp]),
+    "qgb_stream_create": (i32, [C.POINTER(vp)]),
+    "qgb_stream_destroy": (i32, [vp]),
+    "qgb_event_query": (i32, [vp]),
+    "qgb_program_create": (i32, [i32, i32, C.POINTER(QgbOp), i32, dp, i32, C.POINTER(vp)]),
+    "qgb_program_passes": (i32, [vp, ip]),
+    "qgb_program_update": (i32, [vp, C.POINTER(QgbOp), i32, dp, vp]),
+    "qgb_program_run": (i32, [vp, vp, vp]),
+    "qgb_program_destroy": (i32, [vp]),
+    "qgb_batch_create": (i32, [sz, C.POINTER(vp)]),
+    "qgb_batch_run": (i32, [vp, C.c_void_p, i32, i32, vp]),
+    "qgb_batch_destroy": (i32, [vp]),
     "qgb_event_create": (i32, [C.POINTER(vp)]),
     "qgb_event_destroy": (i32, [vp]),
     "qgb_event_record": (i32, [vp, vp]),

@@ -99,6 +99,27 @@ __global__ void __launch_bounds__(256) k_inner(const typename T::S* __restrict__
   }
 }
 
+// <a|b> for states of different precision (complex128 vs complex64)
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(256) k_inner2(const typename TA::S* __restrict__ a, const typename TB::S* __restrict__ b,
+                                                i64 N, double* __restrict__ part) {
+  __shared__ double sh[8];
+  double re = 0.0, im = 0.0;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
+    const typename TA::V x = TA::load(a, i);
+    const typename TB::V y = TB::load(b, i);
+    re += TA::re(x) * TB::re(y) + TA::im(x) * TB::im(y);
+    im += TA::re(x) * TB::im(y) - TA::im(x) * TB::re(y);
+  }
+  re = block_sum_d(re, sh);
+  im = block_sum_d(im, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = re;
+    part[2 * blockIdx.x + 1] = im;
+  }
+}
+
 // out[k] = sum_b part[b * stride + k] for k < nout, fixed order
 __global__ void k_reduce_cols(const double* __restrict__ part, int nrows, int stride, int nout, double* __restrict__ out,
                               double scale) {
@@ -289,6 +310,29 @@ int qgb_inner(const void* a, const void* b, int nqubits, int dtype, double* out,
   if (dtype == QGB_C128) k_inner<TC128><<<blocks, 256, 0, s>>>((const double2*)a, (const double2*)b, N, part);
   else k_inner<TC64><<<blocks, 256, 0, s>>>((const float2*)a, (const float2*)b, N, part);
   QGB_LAUNCH_CHECK("k_inner");
+  k_reduce_cols<<<1, 256, 0, s>>>(part, blocks, 2, 2, out, 1.0);
+  QGB_LAUNCH_CHECK("k_reduce_cols");
+  return QGB_OK;
+}
+
+int qgb_inner_mixed(const void* a, int dtype_a, const void* b, int dtype_b, int nqubits, double* out, void* scratch,
+                    void* stream) {
+  if (!a || !b || !out || !scratch || nqubits < 1 || nqubits > QGB_MAXQ || !dtype_ok(dtype_a) || !dtype_ok(dtype_b)) {
+    qgb_set_error("qgb_inner_mixed: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  if (dtype_a == dtype_b) return qgb_inner(a, b, nqubits, dtype_a, out, scratch, stream);
+  const i64 N = (i64)1 << nqubits;
+  int blocks;
+  grid_for(N, 256, &blocks);
+  blocks = std::min(blocks, kAdjBlocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)scratch;
+  if (dtype_a == QGB_C128)
+    k_inner2<TC128, TC64><<<blocks, 256, 0, s>>>((const double2*)a, (const float2*)b, N, part);
+  else
+    k_inner2<TC64, TC128><<<blocks, 256, 0, s>>>((const float2*)a, (const double2*)b, N, part);
+  QGB_LAUNCH_CHECK("k_inner2");
   k_reduce_cols<<<1, 256, 0, s>>>(part, blocks, 2, 2, out, 1.0);
   QGB_LAUNCH_CHECK("k_reduce_cols");
   return QGB_OK;

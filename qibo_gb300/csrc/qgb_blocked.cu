@@ -20,48 +20,12 @@
 #include <set>
 #include <vector>
 
-#include "qgb_df64.cuh"
-#include "qgb_plan.h"
+#include "qgb_tile.cuh"
 
 #define QGB_PASS_MAX_OPS 96
 #define QGB_PASS_MAX_COEF 1536
 
 int qgb_launch_gateop(void* state, int n, int dtype, const GateOp& g, cudaStream_t s);  // qgb_gates.cu
-
-// Pass traits: G = amplitude type in HBM, S = shared-memory tile element,
-// V = value computed on.  complex64 and strict complex128 compute in their
-// own precision; TC128F (qgb_df64.cuh) keeps complex128 tiles as double-float.
-template <typename C, typename G_>
-struct PlainPass {
-  typedef G_ G;
-  typedef G_ S;
-  typedef G_ V;
-  static V coef(double re, double im) { return C::coef(re, im); }
-  __device__ static V from_global(G v) { return v; }
-  __device__ static G to_global(V v) { return v; }
-  __device__ static V load(const S* p, int i) { return p[i]; }
-  __device__ static void store(S* p, int i, V v) { p[i] = v; }
-  __device__ static V mul(V a, V b) { return cmul(a, b); }
-  template <int D>
-  __device__ static V row(const V* u, const V* a) {
-    V acc = cmul(u[0], a[0]);
-#pragma unroll
-    for (int c = 1; c < D; ++c) acc = cfma(u[c], a[c], acc);
-    return acc;
-  }
-};
-typedef PlainPass<TC64, float2> P64;
-typedef PlainPass<TC128, double2> P128;
-
-struct POp {
-  uint8_t kind, k;
-  uint8_t tpos[5];   // tile-local target positions, most significant matrix bit first
-  uint8_t pad;
-  uint32_t lmask;    // tile-local bits that must be 1 (controls, phase mask)
-  uint64_t gmask;    // non-local index bits that must be 1 (tested per tile)
-  int32_t coef;      // offset into PassParams::coef
-  int32_t pad2;
-};
 
 template <typename T>
 struct PassParams {
@@ -72,46 +36,11 @@ struct PassParams {
   typename T::V coef[QGB_PASS_MAX_COEF];
 };
 
-__device__ __forceinline__ int ins0(int j, int p) { return ((j >> p) << (p + 1)) | (j & ((1 << p) - 1)); }
-
-template <typename T, int K>
-__device__ __forceinline__ void apply_dense_tile(typename T::S* tile, int L, const POp& op,
-                                                 const typename T::V* __restrict__ M) {
-  constexpr int D = 1 << K;
-  int sorted[K];
-#pragma unroll
-  for (int i = 0; i < K; ++i) sorted[i] = op.tpos[i];
-#pragma unroll
-  for (int a = 0; a < K; ++a)
-#pragma unroll
-    for (int b = a + 1; b < K; ++b)
-      if (sorted[b] < sorted[a]) { int t = sorted[a]; sorted[a] = sorted[b]; sorted[b] = t; }
-  int off[D];
-#pragma unroll
-  for (int mm = 0; mm < D; ++mm) {
-    int o = 0;
-#pragma unroll
-    for (int i = 0; i < K; ++i)
-      if ((mm >> (K - 1 - i)) & 1) o |= 1 << op.tpos[i];
-    off[mm] = o;
-  }
-  const int groups = 1 << (L - K);
-  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-    int j0 = g;
-#pragma unroll
-    for (int i = 0; i < K; ++i) j0 = ins0(j0, sorted[i]);
-    if ((j0 & op.lmask) != op.lmask) continue;
-    typename T::V v[D];
-#pragma unroll
-    for (int mm = 0; mm < D; ++mm) v[mm] = T::load(tile, j0 + off[mm]);
-#pragma unroll
-    for (int r = 0; r < D; ++r) T::store(tile, j0 + off[r], T::template row<D>(M + r * D, v));
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_pass(typename T::G* __restrict__ psi, i64 ntiles,
-                                              const __grid_constant__ PassParams<T> P) {
+// One pass over the state (see the file comment); P may live in kernel
+// parameter space (k_pass) or in device memory (k_pass_dev, used by captured
+// programs whose state pointer and coefficients change between replays).
+template <typename T, int MAXK>
+__device__ __forceinline__ void pass_body(typename T::G* __restrict__ psi, i64 ntiles, const PassParams<T>& P) {
   typedef typename T::S S;
   typedef typename T::V V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -138,61 +67,30 @@ __global__ void __launch_bounds__(256) k_pass(typename T::G* __restrict__ psi, i
       const POp& op = P.ops[o];
       if ((base & (i64)op.gmask) != (i64)op.gmask) continue;  // uniform over the CTA
       const V* M = P.coef + op.coef;
-      switch (op.kind) {
-        case GK_PHASE: {
-          const V ph = M[0];
-          for (int j = threadIdx.x; j < TN; j += blockDim.x)
-            if ((j & op.lmask) == op.lmask) T::store(tile, j, T::mul(ph, T::load(tile, j)));
-          break;
-        }
-        case GK_DIAG: {
-          for (int j = threadIdx.x; j < TN; j += blockDim.x) {
-            if ((j & op.lmask) != op.lmask) continue;
-            int mm = 0;
-            for (int i = 0; i < op.k; ++i) mm = (mm << 1) | ((j >> op.tpos[i]) & 1);
-            T::store(tile, j, T::mul(M[mm], T::load(tile, j)));
-          }
-          break;
-        }
-        case GK_XLIKE: {
-          const int p = op.tpos[0];
-          for (int g = threadIdx.x; g < TN / 2; g += blockDim.x) {
-            const int j0 = ins0(g, p), j1 = j0 | (1 << p);
-            if ((j0 & op.lmask) != op.lmask) continue;
-            const V a0 = T::load(tile, j0), a1 = T::load(tile, j1);
-            T::store(tile, j0, T::mul(M[0], a1));
-            T::store(tile, j1, T::mul(M[1], a0));
-          }
-          break;
-        }
-        case GK_SWAP: {
-          const int p0 = min(op.tpos[0], op.tpos[1]), p1 = max(op.tpos[0], op.tpos[1]);
-          for (int g = threadIdx.x; g < TN / 4; g += blockDim.x) {
-            const int j = ins0(ins0(g, p0), p1);
-            if ((j & op.lmask) != op.lmask) continue;
-            const int ja = j | (1 << p0), jb = j | (1 << p1);
-            const S va = tile[ja];
-            tile[ja] = tile[jb];
-            tile[jb] = va;
-          }
-          break;
-        }
-        default: {
-          switch (op.k) {
-            case 1: apply_dense_tile<T, 1>(tile, L, op, M); break;
-            case 2: apply_dense_tile<T, 2>(tile, L, op, M); break;
-            case 3: apply_dense_tile<T, 3>(tile, L, op, M); break;
-            case 4: apply_dense_tile<T, 4>(tile, L, op, M); break;
-            default: apply_dense_tile<T, 5>(tile, L, op, M); break;
-          }
-        }
-      }
+      apply_tile_op<T, MAXK>(tile, L, op, M);
       __syncthreads();
     }
     for (int j = threadIdx.x; j < TN; j += blockDim.x)
       psi[base | dep[j >> m] | (j & lowmask)] = T::to_global(T::load(tile, j));
     __syncthreads();
   }
+}
+
+// Passes whose dense blocks have at most 2 qubits (the common case) are
+// compiled for two resident CTAs per SM; passes with 3-5-qubit fused blocks
+// get the full register file.
+#define QGB_PASS_MIN_CTAS(MAXK) ((MAXK) <= 2 ? 2 : 1)
+
+template <typename T, int MAXK>
+__global__ void __launch_bounds__(256, QGB_PASS_MIN_CTAS(MAXK))
+    k_pass(typename T::G* __restrict__ psi, i64 ntiles, const __grid_constant__ PassParams<T> P) {
+  pass_body<T, MAXK>(psi, ntiles, P);
+}
+
+template <typename T, int MAXK>
+__global__ void __launch_bounds__(256, QGB_PASS_MIN_CTAS(MAXK))
+    k_pass_dev(typename T::G* const* __restrict__ psi_slot, i64 ntiles, const PassParams<T>* __restrict__ P) {
+  pass_body<T, MAXK>(*psi_slot, ntiles, *P);
 }
 
 // ===========================================================================
@@ -257,8 +155,7 @@ std::vector<Pass> plan_passes(const std::vector<GateOp>& ops, int n, int L, int 
 }
 
 template <typename T>
-int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vector<GateOp>& ops, cudaStream_t s) {
-  PassParams<T>* P = new PassParams<T>();
+void pack_params(PassParams<T>* P, int n, int L, int m, const Pass& pass, const std::vector<GateOp>& ops) {
   P->nops = (int)pass.ops.size();
   P->L = L;
   P->m = m;
@@ -284,17 +181,51 @@ int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vect
     po.coef = coef;
     for (const zd& c : g.coef) P->coef[coef++] = T::coef(c.real(), c.imag());
   }
-  const i64 ntiles = (i64)1 << (n - L);
-  const size_t smem = ((size_t)sizeof(typename T::S) << L) + (sizeof(i64) << (L - m));
+}
+
+template <typename T>
+struct PassLaunch {
+  size_t smem;
+  i64 ntiles, blocks;
+  int threads;
+};
+
+template <typename T>
+PassLaunch<T> pass_launch(int n, int L, int m) {
+  PassLaunch<T> pl;
+  pl.ntiles = (i64)1 << (n - L);
+  pl.smem = ((size_t)sizeof(typename T::S) << L) + (sizeof(i64) << (L - m));
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_pass<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_pass<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_pass_dev<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_pass_dev<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr_set = true;
   }
-  const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (smem + 1024)));
-  const i64 blocks = std::min<i64>(ntiles, (i64)qgb_num_sms() * per_sm);
-  const int threads = std::min(256, std::max(32, 1 << L));
-  k_pass<T><<<(unsigned)blocks, threads, smem, s>>>((typename T::G*)state, ntiles, *P);
+  const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (pl.smem + 1024)));
+  pl.blocks = std::min<i64>(pl.ntiles, (i64)qgb_num_sms() * per_sm);
+  pl.threads = std::min(256, std::max(32, 1 << L));
+  return pl;
+}
+
+// largest dense block of a pass (selects the kernel instantiation)
+int pass_maxk(const Pass& pass, const std::vector<GateOp>& ops) {
+  int k = 0;
+  for (int i : pass.ops)
+    if (ops[i].kind == GK_DENSE) k = std::max(k, (int)ops[i].tbits.size());
+  return k;
+}
+
+template <typename T>
+int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vector<GateOp>& ops, cudaStream_t s) {
+  PassParams<T>* P = new PassParams<T>();
+  pack_params<T>(P, n, L, m, pass, ops);
+  const PassLaunch<T> pl = pass_launch<T>(n, L, m);
+  if (pass_maxk(pass, ops) <= 2)
+    k_pass<T, 2><<<(unsigned)pl.blocks, pl.threads, pl.smem, s>>>((typename T::G*)state, pl.ntiles, *P);
+  else
+    k_pass<T, 5><<<(unsigned)pl.blocks, pl.threads, pl.smem, s>>>((typename T::G*)state, pl.ntiles, *P);
   delete P;
   QGB_LAUNCH_CHECK("k_pass");
   return QGB_OK;
@@ -341,3 +272,190 @@ extern "C" int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int no
   *npasses = (int)plan_passes(g, nqubits, L, m).size();
   return QGB_OK;
 }
+
+// ===========================================================================
+// Programs: a planned circuit whose pass parameters and state pointer live in
+// device memory, so the launch sequence is captured once as a CUDA graph and
+// replayed for every circuit of the same shape (same gates on the same
+// qubits; matrices may change through qgb_program_update).
+namespace {
+struct Program {
+  int n, dtype, L, m;
+  bool strict;
+  std::vector<GateOp> ops;
+  std::vector<Pass> passes;
+  size_t pbytes;             // bytes of one PassParams
+  unsigned char* hparams;    // pinned host staging, passes * pbytes
+  void* dparams;             // device copy
+  void** dslot;              // device: the state pointer the kernels read
+  void** hslot;              // pinned host copy of the state pointer
+  cudaEvent_t staged;        // last host->device copy of hparams / hslot
+  cudaGraphExec_t exec;
+  bool captured;
+  bool use_graph;
+};
+
+template <typename T>
+void program_pack(Program* p) {
+  for (size_t i = 0; i < p->passes.size(); ++i)
+    pack_params<T>((PassParams<T>*)(p->hparams + i * p->pbytes), p->n, p->L, p->m, p->passes[i], p->ops);
+}
+
+template <typename T>
+int program_launches(Program* p, cudaStream_t s) {
+  const PassLaunch<T> pl = pass_launch<T>(p->n, p->L, p->m);
+  for (size_t i = 0; i < p->passes.size(); ++i) {
+    const PassParams<T>* P = (const PassParams<T>*)((unsigned char*)p->dparams + i * p->pbytes);
+    if (pass_maxk(p->passes[i], p->ops) <= 2)
+      k_pass_dev<T, 2><<<(unsigned)pl.blocks, pl.threads, pl.smem, s>>>((typename T::G* const*)p->dslot, pl.ntiles, P);
+    else
+      k_pass_dev<T, 5><<<(unsigned)pl.blocks, pl.threads, pl.smem, s>>>((typename T::G* const*)p->dslot, pl.ntiles, P);
+    QGB_LAUNCH_CHECK("k_pass_dev");
+  }
+  return QGB_OK;
+}
+
+int program_launch_any(Program* p, cudaStream_t s) {
+  if (p->dtype == QGB_C64) return program_launches<P64>(p, s);
+  if (p->strict) return program_launches<P128>(p, s);
+  return program_launches<TC128F>(p, s);
+}
+
+void program_pack_any(Program* p) {
+  if (p->dtype == QGB_C64) program_pack<P64>(p);
+  else if (p->strict) program_pack<P128>(p);
+  else program_pack<TC128F>(p);
+}
+
+size_t program_pbytes(int dtype, bool strict) {
+  if (dtype == QGB_C64) return sizeof(PassParams<P64>);
+  return strict ? sizeof(PassParams<P128>) : sizeof(PassParams<TC128F>);
+}
+
+int classify_all(int n, const qgb_op* ops, int nops, const double* coefs, std::vector<GateOp>* out) {
+  out->resize(nops);
+  for (int i = 0; i < nops; ++i) {
+    int st = qgb_classify(n, ops[i].qubits, ops[i].k, ops[i].controls, ops[i].ncontrols, coefs + ops[i].coef_offset,
+                          &(*out)[i], "qgb_program");
+    if (st) return st;
+  }
+  return QGB_OK;
+}
+
+bool same_shape(const GateOp& a, const GateOp& b) {
+  return a.kind == b.kind && a.tbits == b.tbits && a.cbits == b.cbits && a.coef.size() == b.coef.size() &&
+         a.identity == b.identity;
+}
+}  // namespace
+
+extern "C" {
+
+int qgb_program_create(int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs, int flags,
+                       void** prog) {
+  if (!prog || nops <= 0 || !ops || !coefs || !dtype_ok(dtype) || nqubits < 1 || nqubits > QGB_MAXQ) {
+    qgb_set_error("qgb_program_create: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  *prog = nullptr;
+  Program* p = new Program();
+  p->n = nqubits;
+  p->dtype = dtype;
+  p->strict = (flags & QGB_PLAN_STRICT_FP64) != 0;
+  p->use_graph = (flags & QGB_PROGRAM_NO_GRAPH) == 0;
+  p->L = std::min(nqubits, dtype == QGB_C128 ? 12 : 13);
+  p->m = std::min(p->L, dtype == QGB_C128 ? 4 : 5);
+  int st = classify_all(nqubits, ops, nops, coefs, &p->ops);
+  if (st) { delete p; return st; }
+  p->passes = plan_passes(p->ops, nqubits, p->L, p->m);
+  p->pbytes = (program_pbytes(dtype, p->strict) + 255) / 256 * 256;
+  const size_t total = p->pbytes * p->passes.size();
+  cudaError_t e = cudaMallocHost((void**)&p->hparams, total);
+  if (e == cudaSuccess) e = cudaMalloc(&p->dparams, total);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->dslot, sizeof(void*));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&p->hslot, sizeof(void*));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    qgb_program_destroy(p);
+    return qgb_cuda_status(e, "qgb_program_create");
+  }
+  program_pack_any(p);
+  e = cudaMemcpy(p->dparams, p->hparams, total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    qgb_program_destroy(p);
+    return qgb_cuda_status(e, "qgb_program_create");
+  }
+  *prog = p;
+  return QGB_OK;
+}
+
+int qgb_program_passes(void* prog, int* npasses) {
+  if (!prog || !npasses) { qgb_set_error("qgb_program_passes: bad arguments"); return QGB_ERR_INVALID; }
+  *npasses = (int)((Program*)prog)->passes.size();
+  return QGB_OK;
+}
+
+int qgb_program_update(void* prog, const qgb_op* ops, int nops, const double* coefs, void* stream) {
+  Program* p = (Program*)prog;
+  if (!p || !ops || !coefs || nops != (int)p->ops.size()) {
+    qgb_set_error("qgb_program_update: bad arguments or a different gate count");
+    return QGB_ERR_INVALID;
+  }
+  std::vector<GateOp> g;
+  int st = classify_all(p->n, ops, nops, coefs, &g);
+  if (st) return st;
+  for (int i = 0; i < nops; ++i)
+    if (!same_shape(g[i], p->ops[i])) {
+      qgb_set_error("qgb_program_update: op %d has a different shape than the program", i);
+      return QGB_ERR_INVALID;
+    }
+  QGB_TRY_CUDA(cudaEventSynchronize(p->staged));  // the previous copy has left hparams
+  p->ops.swap(g);
+  program_pack_any(p);
+  cudaStream_t s = (cudaStream_t)stream;
+  QGB_TRY_CUDA(cudaMemcpyAsync(p->dparams, p->hparams, p->pbytes * p->passes.size(), cudaMemcpyHostToDevice, s));
+  QGB_TRY_CUDA(cudaEventRecord(p->staged, s));
+  return QGB_OK;
+}
+
+int qgb_program_run(void* prog, void* state, void* stream) {
+  Program* p = (Program*)prog;
+  if (!p || !state) { qgb_set_error("qgb_program_run: bad arguments"); return QGB_ERR_INVALID; }
+  cudaStream_t s = (cudaStream_t)stream;
+  QGB_TRY_CUDA(cudaEventSynchronize(p->staged));
+  *p->hslot = state;
+  QGB_TRY_CUDA(cudaMemcpyAsync(p->dslot, p->hslot, sizeof(void*), cudaMemcpyHostToDevice, s));
+  QGB_TRY_CUDA(cudaEventRecord(p->staged, s));
+  // the legacy default stream cannot be captured: launch directly there
+  if (!p->use_graph || s == nullptr) return program_launch_any(p, s);
+  if (!p->captured) {
+    cudaGraph_t graph;
+    QGB_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int st = program_launch_any(p, s);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (st) return st;
+    if (e != cudaSuccess) return qgb_cuda_status(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&p->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return qgb_cuda_status(e, "cudaGraphInstantiate");
+    p->captured = true;
+  }
+  QGB_TRY_CUDA(cudaGraphLaunch(p->exec, s));
+  qgb_count_launch();
+  return QGB_OK;
+}
+
+int qgb_program_destroy(void* prog) {
+  Program* p = (Program*)prog;
+  if (!p) return QGB_OK;
+  if (p->staged) cudaEventSynchronize(p->staged);
+  if (p->captured) cudaGraphExecDestroy(p->exec);
+  if (p->staged) cudaEventDestroy(p->staged);
+  if (p->dslot) cudaFree(p->dslot);
+  if (p->dparams) cudaFree(p->dparams);
+  if (p->hslot) cudaFreeHost(p->hslot);
+  if (p->hparams) cudaFreeHost(p->hparams);
+  delete p;
+  return QGB_OK;
+}
+
+}  // extern "C"

@@ -380,6 +380,53 @@ __global__ void __launch_bounds__(256) k_draw(const double* __restrict__ probs, 
   }
 }
 
+// Sampling every qubit straight from the state (no 2^n probability vector):
+// chunk sums of |psi|^2 over 64 amplitudes, then an in-chunk recompute.  The
+// in-chunk running sum adds the same FP64 terms in the same order as the
+// chunk sum, so both CDF levels agree.
+template <typename T>
+__global__ void __launch_bounds__(256) k_state_chunk_sums(const typename T::S* __restrict__ psi, i64 N, i64 nchunks,
+                                                          double* __restrict__ chunk) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 c = blockIdx.x * (i64)blockDim.x + threadIdx.x; c < nchunks; c += stride) {
+    double acc = 0.0;
+    const i64 e = imin64(N, (c + 1) * QGB_CHUNK);
+    for (i64 i = c * QGB_CHUNK; i < e; ++i) acc += T::abs2(T::load(psi, i));
+    chunk[c] = acc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_draw_state(const typename T::S* __restrict__ psi, i64 N,
+                                                    const double* __restrict__ cdf, i64 nchunks, i64 nshots,
+                                                    uint32_t k0, uint32_t k1, int64_t* __restrict__ dst) {
+  const double total = cdf[nchunks - 1];
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 s = blockIdx.x * (i64)blockDim.x + threadIdx.x; s < nshots; s += stride) {
+    Philox4 r = philox4x32_10((uint32_t)s, (uint32_t)(s >> 32), 0u, 0u, k0, k1);
+    const double target = u01_53(r.v[0], r.v[1]) * total;
+    i64 lo = 0, hi = nchunks - 1;
+    while (lo < hi) {
+      const i64 mid = (lo + hi) >> 1;
+      if (cdf[mid] > target) hi = mid; else lo = mid + 1;
+    }
+    double run = lo > 0 ? cdf[lo - 1] : 0.0;
+    const i64 b = lo * QGB_CHUNK, e = imin64(N, b + QGB_CHUNK);
+    i64 pick = -1, last_nz = -1;
+    for (i64 i = b; i < e; ++i) {
+      const double p = T::abs2(T::load(psi, i));
+      if (p > 0.0) {
+        last_nz = i;
+        run += p;
+        if (run > target) { pick = i; break; }
+      }
+    }
+    if (pick < 0) pick = last_nz;
+    if (pick < 0) pick = b;
+    dst[s] = pick;
+  }
+}
+
 __global__ void k_philox_fill(uint32_t* out, i64 nblocks4, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nblocks4; t += stride) {
@@ -448,6 +495,36 @@ int qgb_sample(const double* probs, int m, int64_t nshots, uint64_t seed, int64_
   if (counts) k_draw<true><<<blocks, 256, 0, s>>>(probs, nprobs, cdf, nchunks, nshots, k0, k1, counts);
   else k_draw<false><<<blocks, 256, 0, s>>>(probs, nprobs, cdf, nchunks, nshots, k0, k1, samples);
   QGB_LAUNCH_CHECK("k_draw");
+  return QGB_OK;
+}
+
+size_t qgb_sample_state_scratch_bytes(int nqubits) { return qgb_sample_scratch_bytes(nqubits); }
+
+int qgb_sample_state(const void* state, int nqubits, int dtype, int64_t nshots, uint64_t seed, int64_t* samples,
+                     void* scratch, void* stream) {
+  if (!state || nqubits < 1 || nqubits > QGB_MAXQ || !dtype_ok(dtype) || nshots < 0 || !samples || !scratch) {
+    qgb_set_error("qgb_sample_state: bad arguments");
+    return QGB_ERR_INVALID;
+  }
+  if (nshots == 0) return QGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const i64 N = (i64)1 << nqubits;
+  const i64 nchunks = ceil_div(N, QGB_CHUNK);
+  double* cdf = (double*)scratch;
+  int blocks;
+  grid_for(nchunks, 256, &blocks);
+  if (dtype == QGB_C128) k_state_chunk_sums<TC128><<<blocks, 256, 0, s>>>((const double2*)state, N, nchunks, cdf);
+  else k_state_chunk_sums<TC64><<<blocks, 256, 0, s>>>((const float2*)state, N, nchunks, cdf);
+  QGB_LAUNCH_CHECK("k_state_chunk_sums");
+  int st = scan_inplace(cdf, nchunks, cdf + nchunks, s);
+  if (st) return st;
+  grid_for(nshots, 256, &blocks);
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  if (dtype == QGB_C128)
+    k_draw_state<TC128><<<blocks, 256, 0, s>>>((const double2*)state, N, cdf, nchunks, nshots, k0, k1, samples);
+  else
+    k_draw_state<TC64><<<blocks, 256, 0, s>>>((const float2*)state, N, cdf, nchunks, nshots, k0, k1, samples);
+  QGB_LAUNCH_CHECK("k_draw_state");
   return QGB_OK;
 }
 

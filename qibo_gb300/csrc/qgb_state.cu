@@ -89,6 +89,17 @@ int qgb_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream) {
   QGB_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
   return QGB_OK;
 }
+int qgb_host_alloc(void** ptr, size_t bytes) {
+  if (!ptr) { qgb_set_error("qgb_host_alloc: null ptr"); return QGB_ERR_INVALID; }
+  *ptr = nullptr;
+  cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 1);
+  if (e != cudaSuccess) return qgb_cuda_status(e, "cudaMallocHost");
+  return QGB_OK;
+}
+int qgb_host_free(void* ptr) {
+  if (ptr) QGB_TRY_CUDA(cudaFreeHost(ptr));
+  return QGB_OK;
+}
 int qgb_memset_zero(void* ptr, size_t bytes, void* stream) {
   if (bytes) QGB_TRY_CUDA(cudaMemsetAsync(ptr, 0, bytes, (cudaStream_t)stream));
   return QGB_OK;

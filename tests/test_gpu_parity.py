@@ -281,6 +281,41 @@ def test_sampling_chi_square(backend):
     assert chi2_pvalue(np.bincount(s, minlength=2**n), probs) > 1e-4
 
 
+def test_sample_state_equals_probability_sampling(backend):
+    """Shots drawn straight from the state (no 2^n probability vector) are the
+    same draws as shots from the FP64 probability vector."""
+    from qibo_gb300._lib import check
+    from qibo_gb300.device import DeviceArray, DeviceState
+
+    rt = backend.rt
+    for n, dt in ((18, np.complex128), (17, np.complex64)):
+        st = DeviceState.from_numpy(rand_state(n, 31).astype(dt))
+        probs = backend.engine_gb.probabilities(st, list(range(n)))
+        a = DeviceArray((50000,), np.int64, rt)
+        b = DeviceArray((50000,), np.int64, rt)
+        check(rt.lib.qgb_sample(probs.ptr, n, 50000, 99, a.ptr, None, rt.scratch(rt.lib.qgb_sample_scratch_bytes(n)),
+                                rt.stream))
+        check(rt.lib.qgb_sample_state(st.ptr, n, st.code, 50000, 99, b.ptr,
+                                      rt.scratch(rt.lib.qgb_sample_state_scratch_bytes(n)), rt.stream))
+        np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+
+
+def test_mixed_precision_overlap(backend):
+    from qibo_gb300._lib import check
+    from qibo_gb300.device import DeviceArray, DeviceState
+
+    rt = backend.rt
+    psi = rand_state(16, 8)
+    a = DeviceState.from_numpy(psi)
+    b = DeviceState.from_numpy(psi.astype(np.complex64))
+    out = DeviceArray((2,), np.float64, rt)
+    check(rt.lib.qgb_inner_mixed(a.ptr, a.code, b.ptr, b.code, 16, out.ptr,
+                                 rt.scratch(rt.lib.qgb_inner_scratch_bytes()), rt.stream))
+    re, im = out.to_numpy()
+    want = np.vdot(psi, psi.astype(np.complex64).astype(np.complex128))
+    assert abs(re - want.real) < 1e-12 and abs(im - want.imag) < 1e-12
+
+
 def test_sampling_seed_protocol(backend):
     """Same seed -> same draws; zero-probability outcomes never drawn."""
     p = np.array([0.5, 0.0, 0.25, 0.0, 0.0, 0.25, 0.0, 0.0])
