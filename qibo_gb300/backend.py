@@ -76,6 +76,9 @@ class GB300Methods:
         self.blocked = os.environ.get("QIBO_GB300_BLOCKED", "1") != "0"
         # complex128 passes in IEEE FP64 instead of double-float (QIBO_GB300_STRICT_FP64=1)
         self.strict_fp64 = os.environ.get("QIBO_GB300_STRICT_FP64", "0") == "1"
+        # complex64 results renormalised with an FP64 norm after the circuit
+        # (QIBO_GB300_RENORMALIZE=0 turns it off)
+        self.renormalize_c64 = os.environ.get("QIBO_GB300_RENORMALIZE", "1") != "0"
 
     # -- states -----------------------------------------------------------
     def zero_state(self, nqubits, density_matrix=False, dtype=None):
@@ -145,6 +148,8 @@ class GB300Methods:
                     state = DeviceState.from_numpy(arr, dt)
             descs = [d for d in (describe_gate(g, self) for g in circuit.queue) if d is not None]
             self.engine_gb.apply_many(state, descs, blocked=self.blocked, strict_fp64=self.strict_fp64)
+            if state.dtype == np.complex64 and self.renormalize_c64 and descs:
+                self.engine_gb.renormalize(state)
         except DeviceOutOfMemory:
             raise RuntimeError(f"State does not fit in {self.device} memory."
                                "Please switch the execution device to a "

@@ -233,14 +233,12 @@ int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vect
 
 }  // namespace
 
-int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
-                    bool strict_fp64, cudaStream_t s) {
-  std::vector<GateOp> g(nops);
-  for (int i = 0; i < nops; ++i) {
-    int st = qgb_classify(nqubits, ops[i].qubits, ops[i].k, ops[i].controls, ops[i].ncontrols,
-                          coefs + ops[i].coef_offset, &g[i], "qgb_apply_circuit");
-    if (st) return st;
-  }
+int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc.cu
+
+namespace {
+bool is_tc_block(const GateOp& g) { return g.kind == GK_DENSE && g.tbits.size() == 5 && g.cbits.empty(); }
+
+int run_segment(void* state, int nqubits, int dtype, const std::vector<GateOp>& g, bool strict_fp64, cudaStream_t s) {
   // tile: 2^L amplitudes = 64 KB of shared memory; runs of 2^m contiguous amplitudes (256 B)
   const int L = std::min(nqubits, dtype == QGB_C128 ? 12 : 13);
   const int m = std::min(L, dtype == QGB_C128 ? 4 : 5);
@@ -255,6 +253,39 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
       else st = run_pass<TC128F>(state, nqubits, L, m, p, g, s);
     }
     if (st) return st;
+  }
+  return QGB_OK;
+}
+}  // namespace
+
+// Blocked execution.  For complex64, fused 5-qubit blocks (uncontrolled dense
+// 32x32) run on the tensor cores (qgb_tc.cu), one pass each; the gates
+// between two such blocks are planned into shared-memory passes.
+int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
+                    bool strict_fp64, bool use_tc, cudaStream_t s) {
+  std::vector<GateOp> g(nops);
+  for (int i = 0; i < nops; ++i) {
+    int st = qgb_classify(nqubits, ops[i].qubits, ops[i].k, ops[i].controls, ops[i].ncontrols,
+                          coefs + ops[i].coef_offset, &g[i], "qgb_apply_circuit");
+    if (st) return st;
+  }
+  if (!(use_tc && dtype == QGB_C64)) return run_segment(state, nqubits, dtype, g, strict_fp64, s);
+  std::vector<GateOp> seg;
+  for (int i = 0; i <= nops; ++i) {
+    const bool tc = i < nops && is_tc_block(g[i]);
+    if (i == nops || tc) {
+      if (!seg.empty()) {
+        int st = run_segment(state, nqubits, dtype, seg, strict_fp64, s);
+        if (st) return st;
+        seg.clear();
+      }
+      if (tc) {
+        int st = qgb_launch_fused5_tc(state, nqubits, g[i], s);
+        if (st) return st;
+      }
+    } else {
+      seg.push_back(g[i]);
+    }
   }
   return QGB_OK;
 }

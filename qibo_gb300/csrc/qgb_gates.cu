@@ -375,6 +375,13 @@ int qgb_classify(int n, const int* qubits, int k, const int* controls, int nc, c
     seen |= 1ull << q;
     (j < k ? g.tbits : g.cbits).push_back(n - 1 - q);
   }
+  if (!matrix) {
+    // validation only (qubit ranges and repeats): an identity phase
+    g.kind = GK_PHASE;
+    g.coef = {zd(1, 0)};
+    g.identity = true;
+    return QGB_OK;
+  }
   const int D = 1 << k;
   g.coef.resize(D * D);
   for (int i = 0; i < D * D; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
@@ -466,9 +473,9 @@ int qgb_apply_1q(void* state, int nqubits, int dtype, int target, const double* 
   st = qgb_classify(nqubits, &target, 0, nullptr, 0, nullptr, &g, "qgb_apply_1q");  // validation only
   if (st) return st;
   if (target < 0 || target >= nqubits || !matrix) { qgb_set_error("qgb_apply_1q: bad target or matrix"); return QGB_ERR_INVALID; }
+  g = GateOp();
   g.kind = GK_DENSE;
   g.tbits = {nqubits - 1 - target};
-  g.cbits.clear();
   g.coef.resize(4);
   for (int i = 0; i < 4; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
   return launch_any(state, nqubits, dtype, g, stream);
@@ -530,7 +537,7 @@ int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1, const in
 // ---------------------------------------------------------------------------
 // whole circuits
 int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
-                    bool strict_fp64, cudaStream_t s);  // qgb_blocked.cu
+                    bool strict_fp64, bool use_tc, cudaStream_t s);  // qgb_blocked.cu
 
 extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                                  const double* coefs, int flags, void* stream) {
@@ -539,7 +546,8 @@ extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   if (flags & QGB_PLAN_BLOCKED)
-    return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0, s);
+    return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0,
+                           (flags & QGB_PLAN_NO_TC) == 0, s);
   for (int i = 0; i < nops; ++i) {
     const qgb_op& op = ops[i];
     GateOp g;

@@ -110,6 +110,14 @@ class Engine:
         check(self.lib.qgb_norm2(state.ptr, state.nqubits, state.code, out.ptr, scratch, self.rt.stream))
         return float(out.to_numpy()[0])
 
+    def renormalize(self, state: DeviceState) -> float:
+        """Scale the state to unit norm; the norm is accumulated in FP64.
+        Returns the norm before scaling."""
+        nrm = self.norm2(state) ** 0.5
+        if nrm > 0 and abs(nrm - 1.0) > 0:
+            self.scale(state, 1.0 / nrm)
+        return nrm
+
     def scale(self, state: DeviceState, factor: float):
         check(self.lib.qgb_state_scale(state.ptr, state.nqubits, state.code, float(factor), self.rt.stream))
 

@@ -140,6 +140,39 @@ def test_deep_random_circuit_c128_passes(backend, n):
     assert np.max(np.abs(got - want)) < TOL128
 
 
+def test_direct_entry_points(backend):
+    """qgb_apply_1q / _2q / _phase / _swap against the oracle."""
+    from qibo_gb300 import _lib
+    from qibo_gb300._lib import check
+    from qibo_gb300.device import DeviceState
+
+    rt = backend.rt
+    n = 9
+    psi = rand_state(n, 44)
+    u1 = ref.gate_matrix("U3", (0.3, 1.2, -0.7))
+    u2 = ref.gate_matrix("fSim", (0.4, 0.9))
+    for dt in (np.complex128, np.complex64):
+        st = DeviceState.from_numpy(psi.astype(dt))
+        m1 = np.ascontiguousarray(u1).view(np.float64).ravel()
+        m2 = np.ascontiguousarray(u2).view(np.float64).ravel()
+        check(rt.lib.qgb_apply_1q(st.ptr, n, st.code, 6, m1.ctypes.data_as(_lib.dp), rt.stream))
+        check(rt.lib.qgb_apply_2q(st.ptr, n, st.code, 7, 2, m2.ctypes.data_as(_lib.dp), rt.stream))
+        check(rt.lib.qgb_apply_phase(st.ptr, n, st.code, _lib.int_array([1, 5]), 2, 0.6, -0.8, rt.stream))
+        check(rt.lib.qgb_apply_swap(st.ptr, n, st.code, 0, 8, _lib.int_array([3]), 1, rt.stream))
+        want = ref.apply_gate(psi.astype(dt).astype(np.complex128), u1, [6], n)
+        want = ref.apply_gate(want, u2, [7, 2], n)
+        ph = np.eye(4, dtype=complex)
+        ph[3, 3] = 0.6 - 0.8j
+        want = ref.apply_gate(want, ph, [1, 5], n)
+        want = ref.apply_gate_controlled_by(want, ref.gate_matrix("SWAP"), (3,), (0, 8), n)
+        tol = TOL128 if dt == np.complex128 else TOL64
+        assert np.max(np.abs(np.asarray(st) - want)) < tol, dt
+    with pytest.raises(ValueError):
+        check(rt.lib.qgb_apply_phase(st.ptr, n, st.code, _lib.int_array([1, 1]), 2, 1.0, 0.0, rt.stream))
+    with pytest.raises(ValueError):
+        check(rt.lib.qgb_apply_swap(st.ptr, n, st.code, 0, 0, None, 0, rt.stream))
+
+
 def test_unitary_gates_up_to_5_qubits(backend):
     from scipy.stats import unitary_group
 
