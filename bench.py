@@ -19,7 +19,7 @@ back to the host every step.  The line also carries the complex64 run of the
 same circuit with its infidelity against the complex128 state, and a
 bounded sample of the serving stream (circuits/s, p50/p99).
 
-Other workloads (``--workload``): ``qft20``, ``vqe24``, ``serving``,
+Other workloads (``--workload``): ``qft20``, ``vqe24``, ``serving``, ``tc5``,
 ``memlimit``.  ``--impl reference`` times the reference's CPU algorithm (the
 numpy restatement in ``oracle/``, all host cores) on a bounded sample of the
 same workload.
@@ -215,6 +215,90 @@ def serving_sample(nreq: int, rate: float, baseline_req: int):
                                                      "p50_ms": bst["p50_ms"], "p99_ms": bst["p99_ms"]}}
 
 
+def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8):
+    """complex64 legs of the brickwork circuit against complex128.
+
+    ``passes``: the unfused gate list in shared-memory passes.  ``fused_tc``:
+    ``circ.fuse(5)``, whose uncontrolled 5-qubit blocks run on the tensor
+    cores (3xTF32) and the rest in passes; ``runs`` device-timed circuits give
+    p50/p99.  Both results are renormalised in FP64 and compared with the
+    complex128 blocked result (infidelity 1 - |<psi128|psi64>|^2).
+    ``c128_per_gate_ms`` is one run of the plain complex128 per-gate path
+    (IEEE FP64, one kernel per gate), the comparison point of the fused leg."""
+    from qibo_gb300._lib import check
+    from qibo_gb300.backend import GB300Backend, describe_gate
+    from qibo_gb300.device import DeviceArray, DeviceState
+
+    rt, eng, lib = backend.rt, backend.engine_gb, backend.rt.lib
+    b64 = GB300Backend("complex64")
+    st64 = DeviceState(n, "complex64")
+    out = DeviceArray((2,), np.float64, rt)
+    fdescs = [describe_gate(g, b64) for g in circ.fuse(5).queue]
+    n5 = sum(1 for d in fdescs if len(d[0]) == 5 and not d[1])
+
+    def infidelity():
+        check(lib.qgb_inner_mixed(state.ptr, state.code, st64.ptr, st64.code, n, out.ptr,
+                                  rt.scratch(lib.qgb_inner_scratch_bytes()), rt.stream))
+        re, im = out.to_numpy()
+        return 1.0 - (re * re + im * im)
+
+    def timed(dl, reps):
+        ms = []
+        for _ in range(reps):
+            check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
+            ev.start(rt.stream)
+            b64.engine_gb.apply_many(st64, dl, blocked=True)
+            ms.append(ev.stop_ms(rt.stream))
+        return ms
+
+    # complex128 blocked reference state
+    check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
+    eng.apply_many(state, descs, blocked=True)
+    timed(descs, 2)
+    ms_p = timed(descs, 1)[0]
+    norm_p = b64.engine_gb.renormalize(st64)  # FP64 renormalisation of the complex64 result
+    inf_p = infidelity()
+    timed(fdescs, 2)
+    ms_f = sorted(timed(fdescs, runs))
+    norm_f = b64.engine_gb.renormalize(st64)
+    inf_f = infidelity()
+    # the tensor-core kernel alone: 10 launches of the first 5-qubit block
+    tc_gbs = None
+    blk = next((d for d in fdescs if len(d[0]) == 5 and not d[1]), None)
+    if blk is not None:
+        from qibo_gb300 import _lib
+
+        qs = _lib.int_array(blk[0])
+        mat = np.ascontiguousarray(np.asarray(blk[2], dtype=np.complex128)).view(np.float64).ravel()
+        mp = mat.ctypes.data_as(_lib.dp)
+        check(lib.qgb_apply_fused5_tc(st64.ptr, n, qs, mp, rt.stream))
+        ev.start(rt.stream)
+        for _ in range(10):
+            check(lib.qgb_apply_fused5_tc(st64.ptr, n, qs, mp, rt.stream))
+        tc_ms = ev.stop_ms(rt.stream) / 10
+        tc_gbs = 2 * 2**n * 8 / (tc_ms * 1e-3) / 1e9
+    tc_timeout = C.c_int(0)
+    check(lib.qgb_tc_status(C.byref(tc_timeout)))
+    # plain complex128 per-gate path (state reused: the references above are done)
+    check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
+    ev.start(rt.stream)
+    eng.apply_many(state, descs, blocked=False)
+    ms_g = ev.stop_ms(rt.stream)
+    del st64
+    g64, _ = algorithmic_bytes(n, ndense, ncz, 8)
+    p50 = statistics.median(ms_f)
+    p99 = ms_f[min(len(ms_f) - 1, int(np.ceil(0.99 * len(ms_f))) - 1)]
+    return {"passes": {"gate_ms": ms_p, "value": g64 / (ms_p * 1e-3) / 1e9, "unit": "GB/s",
+                       "infidelity_vs_c128": inf_p, "norm_before_renormalisation": norm_p},
+            "fused_tc": {"blocks": len(fdescs), "tc_blocks_5q": n5, "runs": runs, "p50_ms": p50, "p99_ms": p99,
+                         "circuits_per_s": 1e3 / p50, "infidelity_vs_c128": inf_f,
+                         "norm_before_renormalisation": norm_f, "tc_wait_timeouts": tc_timeout.value,
+                         "k_fused5_tc_gbs": tc_gbs, "k_fused5_tc_bytes_per_launch": 2 * 2**n * 8,
+                         "p99_note": "p99 of 8 runs is the slowest run"},
+            "c128_per_gate_ms": ms_g,
+            "fused_tc_speedup_vs_c128_per_gate": ms_g / p50}
+
+
 def run_brickwork(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -332,29 +416,8 @@ def run_brickwork(args):
             "e2e": {"value": total_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": coef_bytes,
                     "d2h_bytes_per_step": NSHOTS * 8, "seconds": e2e_s}}
 
-    if dtype == "complex128" and rank == 0 and not args.quick:
-        # complex64 leg of the same circuit and its infidelity against complex128
-        b64 = GB300Backend("complex64")
-        st64 = DeviceState(n, "complex64")
-        for _ in range(2):
-            check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
-            b64.engine_gb.apply_many(st64, descs, blocked=True)
-        check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
-        ev.start(rt.stream)
-        b64.engine_gb.apply_many(st64, descs, blocked=True)
-        ms64 = ev.stop_ms(rt.stream)
-        norm64 = b64.engine_gb.renormalize(st64)  # FP64 renormalisation of the complex64 result
-        check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
-        eng.apply_many(state, descs, blocked=True)
-        out = DeviceArray((2,), np.float64, rt)
-        check(lib.qgb_inner_mixed(state.ptr, state.code, st64.ptr, st64.code, n, out.ptr,
-                                  rt.scratch(lib.qgb_inner_scratch_bytes()), rt.stream))
-        re, im = out.to_numpy()
-        g64, _ = algorithmic_bytes(n, ndense, ncz, 8)
-        line["complex64"] = {"gate_ms": ms64, "value": g64 / (ms64 * 1e-3) / 1e9, "unit": "GB/s",
-                             "infidelity_vs_c128": 1.0 - (re * re + im * im),
-                             "norm_before_renormalisation": norm64}
-        del st64
+    if dtype == "complex128" and rank == 0 and not args.quick and mode != "fused":
+        line["complex64"] = complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0 and world == 1 and args.serving_requests > 0:
@@ -423,6 +486,48 @@ def run_serving(args):
                       **serving_sample(args.serving_requests or 2000, args.serving_rate, args.serving_baseline)}))
 
 
+def run_tc5(args):
+    """k_fused5_tc alone: a random 5-qubit unitary applied to a complex64
+    state of ``--nqubits`` qubits (default 30, 8.6 GB; inputs >> L2), one
+    launch per step, for three placements of the block qubits (lowest index
+    bits, highest, spread).  Algorithmic bytes per launch: 2 * 2^n * 8."""
+    from qibo_gb300 import _lib
+    from qibo_gb300._lib import check
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+
+    n = args.nqubits
+    b = GB300Backend("complex64")
+    rt, lib = b.rt, b.rt.lib
+    st = DeviceState(n, "complex64")
+    check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+    rng = np.random.default_rng(5)
+    z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
+    u, _ = np.linalg.qr(z)
+    mat = np.ascontiguousarray(u.astype(np.complex128)).view(np.float64).ravel()
+    mp = mat.ctypes.data_as(_lib.dp)
+    peak = measured_peaks().get("hbm_gbs", 6800.0)
+    ev = Events(lib)
+    nbytes = 2 * 2**n * 8
+    out = {}
+    for name, qs in (("high_bits", [0, 1, 2, 3, 4]), ("low_bits", [n - 1, n - 2, n - 3, n - 4, n - 5]),
+                     ("spread", [1, n // 3, n // 2, n - 3, n - 1])):
+        qa = _lib.int_array(qs)
+        for _ in range(args.warmup):
+            check(lib.qgb_apply_fused5_tc(st.ptr, n, qa, mp, rt.stream))
+        ev.start(rt.stream)
+        for _ in range(args.steps):
+            check(lib.qgb_apply_fused5_tc(st.ptr, n, qa, mp, rt.stream))
+        ms = ev.stop_ms(rt.stream) / args.steps
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"qubits": qs, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
+                     "tensor_tflops_3xtf32": 3 * 2 * 64 * 64 * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
+    flag = C.c_int(0)
+    check(lib.qgb_tc_status(C.byref(flag)))
+    print(json.dumps({"workload": f"k_fused5_tc, complex64 n={n}, random 5-qubit unitary", "bytes_per_launch": nbytes,
+                      "hbm_peak_gbs": peak, "tc_wait_timeouts": flag.value, **out}))
+
+
 def run_memlimit(args):
     """33-qubit complex128 (137 GB) and 34-qubit complex64 (137 GB): QFT then
     a depth-10 U3+CZ brickwork in shared-memory passes, 1e7 shots drawn
@@ -483,7 +588,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft20", "vqe24", "serving", "memlimit"])
+    ap.add_argument("--workload", default="brickwork",
+                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused"])
@@ -496,7 +602,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
-            "memlimit": run_memlimit}[args.workload](args)
+            "memlimit": run_memlimit, "tc5": run_tc5}[args.workload](args)
 
 
 if __name__ == "__main__":

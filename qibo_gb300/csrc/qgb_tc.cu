@@ -7,15 +7,30 @@
 // the 64x64 real matrix B with 2x2 blocks [[Ur, -Ui], [Ui, Ur]], so 128
 // groups at a time form a GEMM  D[128 x 64] = A[128 x 64] * B^T.
 //
-// Each CTA (128 threads) gathers 128 groups, splits every value into a TF32
-// head and a remainder (x = hi + lo), writes A_hi / A_lo to shared memory in
-// the no-swizzle K-major core-matrix layout, and one thread issues
+// A CTA (128 threads) owns a tile of 4096 amplitudes: the 5 block bits plus
+// the 7 lowest other index bits.  Tile index j has its 7 low bits equal to
+// global index bits 0..6 (those bits are always in the tile), so thread t
+// loads amplitudes j = t + 128 r, r = 0..31: every warp load is 256
+// contiguous bytes.  Each value is split into a TF32 head and a remainder
+// (x = hi + lo) and written to A_hi / A_lo in shared memory in the K-major
+// no-swizzle core-matrix layout (row = group, column = block index).  One
+// thread issues
 //   D = A_hi*B_hi + A_hi*B_lo + A_lo*B_hi     (3xTF32, FP32 accumulation)
 // as 24 tcgen05.mma.kind::tf32 instructions (M=128, N=64, K=8) into tensor
-// memory.  Completion is signalled through an mbarrier; thread t then reads
-// TMEM lane t -- the output row of the very group it gathered -- with
-// tcgen05.ld and scatters it back.  Every wait on the mbarrier is bounded:
-// on timeout the kernel records an error flag, stops issuing work, frees its
+// memory and commits them to an mbarrier; meanwhile every thread loads the
+// next tile into registers.  Thread t then reads TMEM lane t (group t's 32
+// outputs) with tcgen05.ld, stages them in shared memory in tile order, and
+// the CTA stores the tile back with the same coalesced pattern.
+//
+// Bank conflicts.  Core matrices are padded (row-group stride 144 B, K-chunk
+// stride 2320 B) so that both strides rotate the 16-byte bank group by one;
+// the block matrix is permuted (U -> P U P^T) so that the block qubits on the
+// lowest index bits take the lowest column bits; and the staging buffer is
+// XOR-swizzled in its low 4 index bits.  Every warp access then spreads
+// over the banks whatever the block's qubits are.
+//
+// Every wait on the mbarrier is bounded: on timeout the kernel records an
+// error flag, waits once more (bounded) for the in-flight MMAs, frees its
 // tensor memory and returns.
 #include <algorithm>
 #include <vector>
@@ -26,35 +41,61 @@
 #define TC_N 64
 #define TC_K 64
 #define TC_THREADS 128
-// shared memory layout (bytes); each operand region is padded so that the
-// descriptor reads stay inside the allocation for either assignment of the
-// leading/stride byte offsets
-#define TC_A_BYTES (TC_M * TC_K * 4)          // 32 KB
-#define TC_B_BYTES (TC_N * TC_K * 4)          // 16 KB
+#define TC_TILE 4096  // amplitudes per tile (128 groups x 32)
+// K-major, no swizzle: 8-row x 16-byte core matrices; core matrices adjacent
+// along K are LBO bytes apart, along M/N SBO bytes apart.  A is padded by 16
+// bytes per row group and by 16*rot bytes per K chunk, rot in {1, 2, 4}
+// chosen per block (bank rotation); B is written once per CTA and stays
+// dense.
+#define TC_A_SBO 144
+#define TC_A_LBO0 (TC_M / 8 * TC_A_SBO)  // 2304 = 0 mod 128
+#define TC_A_LBO_MAX (TC_A_LBO0 + 64)
+#define TC_B_SBO 128
+#define TC_B_LBO (TC_N / 8 * TC_B_SBO)  // 1024
+// shared memory layout (bytes)
+#define TC_A_BYTES (TC_K / 4 * TC_A_LBO_MAX)  // 37888
+#define TC_B_BYTES (TC_K / 4 * TC_B_LBO)  // 16384
 #define TC_OFF_AHI 0
-#define TC_OFF_ALO (TC_OFF_AHI + TC_A_BYTES)  // 32 KB
-#define TC_OFF_BHI (TC_OFF_ALO + TC_A_BYTES)  // 64 KB
-#define TC_OFF_BLO (TC_OFF_BHI + TC_B_BYTES)  // 80 KB
-// 96 KB of operands + 8 KB guard: with LBO/SBO exchanged the farthest read is
-// B_lo + 7*2*128 + 7*1024 + 128 + 124 = 101.7 KB, still inside
-#define TC_SMEM (TC_OFF_BLO + TC_B_BYTES + 8 * 1024)
+#define TC_OFF_ALO (TC_OFF_AHI + TC_A_BYTES)
+#define TC_OFF_BHI (TC_OFF_ALO + TC_A_BYTES)
+#define TC_OFF_BLO (TC_OFF_BHI + TC_B_BYTES)
+#define TC_SMEM (TC_OFF_BLO + TC_B_BYTES)  // 108 544
 #define TC_SPIN_LIMIT (1u << 26)
 
-// K-major, no swizzle: 8-row x 16-byte core matrices; core matrices adjacent
-// along K are LBO bytes apart, along M/N SBO bytes apart.
-#define TC_A_SBO 128
-#define TC_A_LBO (TC_M / 8 * 128)  // 2048: all 16 row-groups of one K-chunk
-#define TC_B_SBO 128
-#define TC_B_LBO (TC_N / 8 * 128)  // 1024
+static_assert(TC_TILE * 8 <= TC_A_BYTES, "staging buffer must fit in A_hi");
+static_assert(TC_A_BYTES % 16 == 0 && TC_B_BYTES % 16 == 0, "operand regions 16-byte aligned");
 
 struct TcGate {
   float ur[32][32];
   float ui[32][32];
 };
 
-struct Offs32 {
-  i64 o[32];
+// Tile geometry.  Tile index j = t + 128 r (thread t, step r); its global
+// offset is base(tile) + t + ghi[r] (index bits 0..6 are the tile's low
+// bits).  Shared-memory byte offset of j in A is aoff_lo[t] + aoff_hi[r]
+// (the core-matrix offset is additive over disjoint row / column bits).
+// Staging slot of (group row, block column c) is
+//   (c << 7 | row) ^ ((c << g) & 15),   g = 4 - (block qubits on bits 0..3),
+// a bijection on [0, 4096) that is linear over disjoint bits: the epilogue
+// writes row ^ scol[c], the store reads sread_lo[t] ^ sread_hi[r].  Within a
+// half-warp both patterns cover 16 distinct 8-byte slots.
+struct TcGeom {
+  int nbits;           // bits in a tile (12, fewer for small states)
+  int nrest;           // remaining index bits
+  int rest[QGB_MAXQ];  // their global positions, ascending
+  uint32_t a_lbo;      // K-chunk stride of A: TC_A_LBO0 + 16 * rot
+  i64 ghi[32];
+  uint32_t aoff_lo[128];
+  uint32_t aoff_hi[32];
+  uint16_t sread_lo[128];
+  uint16_t sread_hi[32];
+  uint16_t scol[32];
 };
+
+__host__ __device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t k, uint32_t lbo, uint32_t sbo) {
+  // byte offset of element (row, k) in a K-major no-swizzle operand
+  return (k >> 2) * lbo + (row >> 3) * sbo + (row & 7) * 16 + (k & 3) * 4;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -71,11 +112,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 // kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major, N, M
 __host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ uint32_t core_off(int row, int k, int lbo) {
-  // byte offset of element (row, k) in a K-major no-swizzle operand
-  return (uint32_t)((k >> 2) * lbo + (row >> 3) * 128 + (row & 7) * 16 + (k & 3) * 4);
 }
 
 __device__ __forceinline__ float tf32_head(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
@@ -104,19 +140,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ i64 tile_base(i64 t, const TcGeom& geo) {
+  i64 base = 0;
+  for (int b = 0; b < geo.nrest; ++b) base |= ((t >> b) & 1) << geo.rest[b];
+  return base;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 2)
-    k_fused5_tc(float2* __restrict__ psi, i64 ngroups, BitInsert bi, Offs32 off, const __grid_constant__ TcGate G,
-                int* __restrict__ err) {
+    k_fused5_tc(float2* __restrict__ psi, i64 ntiles, const __grid_constant__ TcGeom geo,
+                const __grid_constant__ TcGate G, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t s_base = smem_u32(sm);
   const uint32_t mb = smem_u32(&mbar);
 
-  // B = realified U, split into TF32 head and remainder; row n = output real,
-  // column k = input real
+  // B = realified (permuted) U, split into TF32 head and remainder; row n =
+  // output real, column k = input real
   for (int e = tid; e < TC_N * TC_K; e += TC_THREADS) {
     const int n = e / TC_K, k = e % TC_K;
     const int r = n >> 1, c = k >> 1;
@@ -124,8 +166,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     if ((n & 1) == 0) v = (k & 1) == 0 ? G.ur[r][c] : -G.ui[r][c];
     else v = (k & 1) == 0 ? G.ui[r][c] : G.ur[r][c];
     const float h = tf32_head(v);
-    *(float*)(sm + TC_OFF_BHI + core_off(n, k, TC_B_LBO)) = h;
-    *(float*)(sm + TC_OFF_BLO + core_off(n, k, TC_B_LBO)) = v - h;
+    const uint32_t o = core_off(n, k, TC_B_LBO, TC_B_SBO);
+    *(float*)(sm + TC_OFF_BHI + o) = h;
+    *(float*)(sm + TC_OFF_BLO + o) = v - h;
   }
   if (tid == 0) {
     abort_flag = 0;
@@ -143,23 +186,36 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   const uint32_t tmem = tmem_base;
   constexpr uint32_t IDESC = tc_idesc(TC_M, TC_N);
   uint32_t phase = 0;
+  const int TN = 1 << geo.nbits;
+  const int nr = TN >= TC_THREADS ? TN / TC_THREADS : 1;  // steps per thread
+  const bool tval = tid < TN;                             // this thread has elements
+  const int nrows = TN >> 5;
+  const uint32_t aoff = geo.aoff_lo[tid];
+  const uint32_t srd = geo.sread_lo[tid];
+  const uint32_t a_lbo = geo.a_lbo;
+  float2* stage = (float2*)(sm + TC_OFF_AHI);
 
-  const i64 ntiles = (ngroups + TC_M - 1) / TC_M;
-  for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    // gather one group per thread and write A_hi / A_lo
-    const i64 g = t * TC_M + tid;
-    const bool valid = g < ngroups;
-    const i64 base = valid ? insert_zeros(g, bi) : 0;
-    float2 x[32];
+  float2 v[32];
+  i64 t = blockIdx.x;
+  i64 base = 0;
+  if (t < ntiles) {
+    base = tile_base(t, geo);
+    const float2* src = psi + base + tid;
 #pragma unroll
-    for (int c = 0; c < 32; ++c) x[c] = valid ? psi[base + off.o[c]] : make_float2(0.f, 0.f);
+    for (int r = 0; r < 32; ++r)
+      if (tval && r < nr) v[r] = src[geo.ghi[r]];
+  }
+  for (; t < ntiles; t += gridDim.x) {
+    // registers -> A_hi / A_lo (row = group, columns 2c, 2c+1 = re, im of element c)
 #pragma unroll
-    for (int c = 0; c < 32; c += 2) {
-      const float4 v = make_float4(x[c].x, x[c].y, x[c + 1].x, x[c + 1].y);
-      const float4 h = make_float4(tf32_head(v.x), tf32_head(v.y), tf32_head(v.z), tf32_head(v.w));
-      const uint32_t o = core_off(tid, 2 * c, TC_A_LBO);
-      *(float4*)(sm + TC_OFF_AHI + o) = h;
-      *(float4*)(sm + TC_OFF_ALO + o) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+    for (int r = 0; r < 32; ++r) {
+      if (tval && r < nr) {
+        const float2 x = v[r];
+        const float2 h = make_float2(tf32_head(x.x), tf32_head(x.y));
+        const uint32_t o = aoff + geo.aoff_hi[r];
+        *(float2*)(sm + TC_OFF_AHI + o) = h;
+        *(float2*)(sm + TC_OFF_ALO + o) = make_float2(x.x - h.x, x.y - h.y);
+      }
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -169,50 +225,64 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
       uint32_t acc = 0;
 #pragma unroll
       for (int s = 0; s < TC_K / 8; ++s) {
-        const uint64_t ahi = smem_desc(s_base + TC_OFF_AHI + s * 2 * TC_A_LBO, TC_A_LBO, TC_A_SBO);
-        const uint64_t alo = smem_desc(s_base + TC_OFF_ALO + s * 2 * TC_A_LBO, TC_A_LBO, TC_A_SBO);
+        const uint64_t ahi = smem_desc(s_base + TC_OFF_AHI + s * 2 * a_lbo, a_lbo, TC_A_SBO);
+        const uint64_t alo = smem_desc(s_base + TC_OFF_ALO + s * 2 * a_lbo, a_lbo, TC_A_SBO);
         const uint64_t bhi = smem_desc(s_base + TC_OFF_BHI + s * 2 * TC_B_LBO, TC_B_LBO, TC_B_SBO);
         const uint64_t blo = smem_desc(s_base + TC_OFF_BLO + s * 2 * TC_B_LBO, TC_B_LBO, TC_B_SBO);
         const uint64_t as[3] = {ahi, ahi, alo};
         const uint64_t bs[3] = {bhi, blo, bhi};
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
+        for (int q = 0; q < 3; ++q) {
           asm volatile(
               "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
               " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-              "l"(as[j]), "l"(bs[j]), "r"(IDESC), "r"(acc));
+              "l"(as[q]), "l"(bs[q]), "r"(IDESC), "r"(acc));
           acc = 1;
         }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
                    : "memory");
     }
-    const bool ok = mbar_wait(mb, phase);
-    if (!ok) {
-      if (lane == 0) atomicExch(&abort_flag, 1);
+    // prefetch the next tile into registers while the MMAs run
+    const i64 tn = t + gridDim.x;
+    i64 nbase = 0;
+    if (tn < ntiles) {
+      nbase = tile_base(tn, geo);
+      const float2* src = psi + nbase + tid;
+#pragma unroll
+      for (int r = 0; r < 32; ++r)
+        if (tval && r < nr) v[r] = src[geo.ghi[r]];
     }
+    const bool ok = mbar_wait(mb, phase);
+    if (!ok) atomicExch(&abort_flag, 1);
     __syncthreads();
     if (abort_flag) {
-      // record the failure, give the in-flight MMA one more bounded wait so
-      // tensor memory is not freed under it, then leave
+      // record the failure, give the in-flight MMAs one more bounded wait so
+      // tensor memory is not freed under them, then leave
       if (tid == 0) atomicExch(err, 1);
       mbar_wait(mb, phase);
       break;
     }
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // TMEM lane (32*warp + lane) holds this thread's group
+    // TMEM lane (32*warp + lane) = row tid = this thread's group
     float y[64];
     const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
     for (int q = 0; q < 4; ++q) tmem_ld16(ta + q * 16, y + q * 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    if (valid) {
+    if (tid < nrows) {
 #pragma unroll
-      for (int c = 0; c < 32; ++c) psi[base + off.o[c]] = make_float2(y[2 * c], y[2 * c + 1]);
+      for (int c = 0; c < 32; ++c) stage[tid ^ geo.scol[c]] = make_float2(y[2 * c], y[2 * c + 1]);
     }
+    __syncthreads();
+    float2* dst = psi + base + tid;
+#pragma unroll
+    for (int r = 0; r < 32; ++r)
+      if (tval && r < nr) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
+    base = nbase;
   }
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_N));
@@ -220,43 +290,111 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 
 namespace {
 int* g_tc_err = nullptr;
+
+// Tile geometry of a block on target bits tbits (matrix order: tbits[0] is
+// the most significant bit of the block index) of an n-qubit state.  Column
+// bit cbit[jt] of the permuted block matrix belongs to target jt: targets
+// are ranked by index position, lowest first.
+void make_geom(int n, const std::vector<int>& tbits, TcGeom* geo, int cbit[5]) {
+  std::vector<int> sorted_t = tbits;
+  std::sort(sorted_t.begin(), sorted_t.end());
+  for (int jt = 0; jt < 5; ++jt)
+    cbit[jt] = (int)(std::find(sorted_t.begin(), sorted_t.end(), tbits[jt]) - sorted_t.begin());
+  std::vector<int> grp;
+  for (int b = 0; b < n && (int)grp.size() < 7; ++b)
+    if (std::find(tbits.begin(), tbits.end(), b) == tbits.end()) grp.push_back(b);
+  std::vector<int> pos = tbits;
+  pos.insert(pos.end(), grp.begin(), grp.end());
+  std::sort(pos.begin(), pos.end());
+  const int nb = (int)pos.size();
+  geo->nbits = nb;
+  // tile bit i -> group-row bit or block-column bit
+  std::vector<int> rowbit(nb, -1), colbit(nb, -1);
+  for (int i = 0; i < nb; ++i) {
+    auto g = std::find(grp.begin(), grp.end(), pos[i]);
+    if (g != grp.end()) rowbit[i] = (int)(g - grp.begin());
+    else colbit[i] = cbit[std::find(tbits.begin(), tbits.end(), pos[i]) - tbits.begin()];
+  }
+  // t4 block qubits on index bits 0..3 (the lanes of a half-warp) take
+  // column bits 0..t4-1, the rest of those lanes group rows 0..3-t4.  A
+  // K-chunk stride that rotates the bank group by 2^(4-t4) (mod 8) then
+  // makes every half-warp write of A hit 16 distinct 8-byte slots (t4 >= 1;
+  // with t4 = 0 the column is fixed and 2 wavefronts are the minimum).
+  int t4 = 0;
+  for (int b : tbits) t4 += b < 4;
+  const uint32_t rot = t4 >= 4 ? 1 : t4 == 3 ? 2 : t4 == 2 ? 4 : 1;
+  geo->a_lbo = TC_A_LBO0 + 16 * rot;
+  const int gsh = 4 - t4;
+  auto scol = [&](uint32_t c) { return (uint32_t)((c << 7) ^ ((c << gsh) & 15u)); };
+  auto split = [&](int bits, int first, int count, i64* dep, uint32_t* row, uint32_t* col) {
+    *dep = 0;
+    *row = 0;
+    *col = 0;
+    for (int i = 0; i < count; ++i) {
+      const int b = first + i;
+      if (b >= nb || !((bits >> i) & 1)) continue;
+      *dep |= (i64)1 << pos[b];
+      if (rowbit[b] >= 0) *row |= 1u << rowbit[b];
+      else *col |= 1u << colbit[b];
+    }
+  };
+  for (int v = 0; v < 128; ++v) {
+    i64 dep;
+    uint32_t row, col;
+    split(v, 0, 7, &dep, &row, &col);
+    geo->aoff_lo[v] = core_off(row, 2 * col, geo->a_lbo, TC_A_SBO);
+    geo->sread_lo[v] = (uint16_t)(row ^ scol(col));
+  }
+  for (int r = 0; r < 32; ++r) {
+    i64 dep;
+    uint32_t row, col;
+    split(r, 7, 5, &dep, &row, &col);
+    geo->ghi[r] = dep;
+    geo->aoff_hi[r] = core_off(row, 2 * col, geo->a_lbo, TC_A_SBO);
+    geo->sread_hi[r] = (uint16_t)(row ^ scol(col));
+    geo->scol[r] = (uint16_t)scol((uint32_t)r);
+  }
+  geo->nrest = 0;
+  for (int b = 0; b < n; ++b)
+    if (std::find(pos.begin(), pos.end(), b) == pos.end()) geo->rest[geo->nrest++] = b;
 }
+}  // namespace
 
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
-  if (g.tbits.size() != 5 || !g.cbits.empty()) {
+  if (g.tbits.size() != 5 || !g.cbits.empty() || n < 5) {
     qgb_set_error("qgb_apply_fused5_tc: needs an uncontrolled 5-qubit dense block");
     return QGB_ERR_INVALID;
   }
   if (!g_tc_err) QGB_TRY_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
   QGB_TRY_CUDA(cudaMemsetAsync(g_tc_err, 0, sizeof(int), s));
-  BitInsert bi;
-  std::vector<int> t = g.tbits;
-  std::sort(t.begin(), t.end());
-  bi.n = 5;
-  for (int j = 0; j < 5; ++j) bi.pos[j] = t[j];
-  Offs32 off;
-  for (int m = 0; m < 32; ++m) {
-    i64 o = 0;
-    for (int j = 0; j < 5; ++j)
-      if ((m >> (4 - j)) & 1) o |= (i64)1 << g.tbits[j];
-    off.o[m] = o;
+  TcGeom* geo = new TcGeom();
+  int cbit[5];
+  make_geom(n, g.tbits, geo, cbit);
+  // permuted block matrix U'[r'][c'] = U[i(r')][i(c')], i(c') the block
+  // index whose bit (4 - jt) is bit cbit[jt] of c'
+  int idx[32];
+  for (int c = 0; c < 32; ++c) {
+    idx[c] = 0;
+    for (int jt = 0; jt < 5; ++jt)
+      if ((c >> cbit[jt]) & 1) idx[c] |= 1 << (4 - jt);
   }
   TcGate* G = new TcGate();
   for (int r = 0; r < 32; ++r)
     for (int c = 0; c < 32; ++c) {
-      G->ur[r][c] = (float)g.coef[r * 32 + c].real();
-      G->ui[r][c] = (float)g.coef[r * 32 + c].imag();
+      const zd u = g.coef[idx[r] * 32 + idx[c]];
+      G->ur[r][c] = (float)u.real();
+      G->ui[r][c] = (float)u.imag();
     }
-  const i64 ngroups = (i64)1 << (n - 5);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_fused5_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     attr = true;
   }
-  const i64 ntiles = (ngroups + TC_M - 1) / TC_M;
+  const i64 ntiles = (i64)1 << (n - geo->nbits);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
-  k_fused5_tc<<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ngroups, bi, off, *G, g_tc_err);
+  k_fused5_tc<<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
   delete G;
+  delete geo;
   QGB_LAUNCH_CHECK("k_fused5_tc");
   return QGB_OK;
 }
@@ -280,7 +418,10 @@ int qgb_apply_fused5_tc(void* state, int nqubits, const int* qubits, const doubl
 }
 
 int qgb_tc_status(int* timed_out) {
-  if (!timed_out) { qgb_set_error("qgb_tc_status: null"); return QGB_ERR_INVALID; }
+  if (!timed_out) {
+    qgb_set_error("qgb_tc_status: null");
+    return QGB_ERR_INVALID;
+  }
   *timed_out = 0;
   if (g_tc_err) QGB_TRY_CUDA(cudaMemcpy(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
   return QGB_OK;

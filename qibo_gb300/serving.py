@@ -447,6 +447,25 @@ class Server:
                 "mean_ms": float(lat.mean() * 1e3), **dict(self.stats)}
 
 
+def shard_requests(requests: List[Request], rank: int, world: int) -> List[Request]:
+    """Replica sharding: one GPU per rank, requests dealt round-robin by id so
+    every rank gets the same mix; no data moves between ranks."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    return [r for r in requests if r.rid % world == rank]
+
+
+def merge_stats(per_rank: List[dict]) -> dict:
+    """Whole-job numbers from per-replica ``Server.run`` stats: requests add
+    up, the wall time is the slowest replica's, latency percentiles are the
+    worst replica's (an upper bound on the pooled percentile)."""
+    n = sum(s["requests"] for s in per_rank)
+    wall = max(s["wall_s"] for s in per_rank)
+    return {"requests": n, "wall_s": wall, "circuits_per_s": n / wall if wall > 0 else float("inf"),
+            "p50_ms": max(s["p50_ms"] for s in per_rank), "p99_ms": max(s["p99_ms"] for s in per_rank),
+            "replicas": len(per_rank)}
+
+
 def make_stream(nreq: int, rate: float, seed: int = 0, nmin: int = 10, nmax: int = 28, dmin: int = 5,
                 dmax: int = 30, nshots: int = 10_000) -> List[Request]:
     """The serving workload: Poisson arrivals at ``rate`` per second; qubits
