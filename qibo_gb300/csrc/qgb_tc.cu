@@ -7,29 +7,31 @@
 // the 64x64 real matrix B with 2x2 blocks [[Ur, -Ui], [Ui, Ur]], so 128
 // groups at a time form a GEMM  D[128 x 64] = A[128 x 64] * B^T.
 //
-// A CTA (128 threads) owns a tile of 4096 amplitudes: the 5 block bits plus
-// the 7 lowest other index bits.  Tile index j has its 7 low bits equal to
-// global index bits 0..6 (those bits are always in the tile), so thread t
-// loads amplitudes j = t + 128 r, r = 0..31: every warp load is 256
-// contiguous bytes.  Each value is split into a TF32 head and a remainder
-// (x = hi + lo) and written to A_hi / A_lo in shared memory in the K-major
-// no-swizzle core-matrix layout (row = group, column = block index).  One
-// thread issues
+// A CTA (256 threads, two per SM) owns a tile of 4096 amplitudes: the 5
+// block bits plus the 7 lowest other index bits.  Tile index j has its 7 low
+// bits equal to global index bits 0..6 (those bits are always in the tile),
+// so thread t loads amplitudes j = t + 256 r, r = 0..15: every warp load is
+// 256 contiguous bytes.  Each value is split into a TF32 head and a
+// remainder (x = hi + lo) and written to A_hi / A_lo in shared memory in the
+// K-major no-swizzle core-matrix layout (row = group, column = block index).
+// One thread issues
 //   D = A_hi*B_hi + A_hi*B_lo + A_lo*B_hi     (3xTF32, FP32 accumulation)
 // as 24 tcgen05.mma.kind::tf32 instructions (M=128, N=64, K=8) into tensor
-// memory and commits them to an mbarrier; meanwhile every thread loads the
-// next tile into registers.  Thread t then reads TMEM lane t (group t's 32
-// outputs) with tcgen05.ld, stages them in shared memory in tile order, and
-// the CTA stores the tile back with the same coalesced pattern.
+// memory, commits them to an mbarrier and waits on it; meanwhile the other
+// threads load the next tile into registers and park at the CTA barrier.
+// Warps w and w+4 then read TMEM lanes 32(w%4).. (the groups) in two column
+// halves with tcgen05.ld, stage the outputs in shared memory in tile order,
+// and the CTA stores the tile back with the coalesced pattern of the load.
 //
 // Bank conflicts.  Core matrices are padded (row-group stride 144 B, K-chunk
-// stride 2320 B) so that both strides rotate the 16-byte bank group by one;
-// the block matrix is permuted (U -> P U P^T) so that the block qubits on the
-// lowest index bits take the lowest column bits; and the staging buffer is
-// XOR-swizzled in its low 4 index bits.  Every warp access then spreads
-// over the banks whatever the block's qubits are.
+// stride 2304 + 16*rot B) so that both strides rotate the 16-byte bank
+// group; the block matrix is permuted (U -> P U P^T) so that the block
+// qubits on the lowest index bits take the lowest column bits; and the
+// staging buffer is XOR-swizzled in its low 4 index bits.  Every half-warp
+// access then covers 16 distinct 8-byte slots (one wavefront), except the
+// A write of a block with no qubit on index bits 0..3 (two).
 //
-// Every wait on the mbarrier is bounded: on timeout the kernel records an
+// The wait on the mbarrier is bounded: on timeout the kernel records an
 // error flag, waits once more (bounded) for the in-flight MMAs, frees its
 // tensor memory and returns.
 #include <algorithm>
@@ -40,7 +42,8 @@
 #define TC_M 128
 #define TC_N 64
 #define TC_K 64
-#define TC_THREADS 128
+#define TC_THREADS 256
+#define TC_STEPS 16   // amplitudes per thread per tile
 #define TC_TILE 4096  // amplitudes per tile (128 groups x 32)
 // K-major, no swizzle: 8-row x 16-byte core matrices; core matrices adjacent
 // along K are LBO bytes apart, along M/N SBO bytes apart.  A is padded by 16
@@ -54,7 +57,7 @@
 #define TC_B_LBO (TC_N / 8 * TC_B_SBO)  // 1024
 // shared memory layout (bytes)
 #define TC_A_BYTES (TC_K / 4 * TC_A_LBO_MAX)  // 37888
-#define TC_B_BYTES (TC_K / 4 * TC_B_LBO)  // 16384
+#define TC_B_BYTES (TC_K / 4 * TC_B_LBO)      // 16384
 #define TC_OFF_AHI 0
 #define TC_OFF_ALO (TC_OFF_AHI + TC_A_BYTES)
 #define TC_OFF_BHI (TC_OFF_ALO + TC_A_BYTES)
@@ -64,31 +67,34 @@
 
 static_assert(TC_TILE * 8 <= TC_A_BYTES, "staging buffer must fit in A_hi");
 static_assert(TC_A_BYTES % 16 == 0 && TC_B_BYTES % 16 == 0, "operand regions 16-byte aligned");
+static_assert(TC_THREADS * TC_STEPS == TC_TILE, "one amplitude per thread and step");
+static_assert(QGB_MAXQ - 12 <= 32, "rest bits are spread over one warp's lanes");
 
 struct TcGate {
   float ur[32][32];
   float ui[32][32];
 };
 
-// Tile geometry.  Tile index j = t + 128 r (thread t, step r); its global
-// offset is base(tile) + t + ghi[r] (index bits 0..6 are the tile's low
-// bits).  Shared-memory byte offset of j in A is aoff_lo[t] + aoff_hi[r]
-// (the core-matrix offset is additive over disjoint row / column bits).
-// Staging slot of (group row, block column c) is
+// Tile geometry.  Tile index j = t + 256 r (thread t, step r); its global
+// offset is base(tile) + (t & 127) + (t >> 7) * g7 + ghi[r] (tile bits 0..6
+// are index bits 0..6; g7 is the offset of tile bit 7).  Shared-memory byte
+// offset of j in A is aoff_lo[t] + aoff_hi[r] (the core-matrix offset is
+// additive over disjoint row / column bits).  Staging slot of (group row,
+// block column c) is
 //   (c << 7 | row) ^ ((c << g) & 15),   g = 4 - (block qubits on bits 0..3),
 // a bijection on [0, 4096) that is linear over disjoint bits: the epilogue
-// writes row ^ scol[c], the store reads sread_lo[t] ^ sread_hi[r].  Within a
-// half-warp both patterns cover 16 distinct 8-byte slots.
+// writes row ^ scol[c], the store reads sread_lo[t] ^ sread_hi[r].
 struct TcGeom {
-  int nbits;           // bits in a tile (12, fewer for small states)
-  int nrest;           // remaining index bits
-  int rest[QGB_MAXQ];  // their global positions, ascending
-  uint32_t a_lbo;      // K-chunk stride of A: TC_A_LBO0 + 16 * rot
-  i64 ghi[32];
-  uint32_t aoff_lo[128];
-  uint32_t aoff_hi[32];
-  uint16_t sread_lo[128];
-  uint16_t sread_hi[32];
+  int nbits;         // bits in a tile (12, fewer for small states)
+  int nrest;         // remaining index bits (at most 28)
+  int rest[32];      // their global positions, ascending
+  uint32_t a_lbo;    // K-chunk stride of A: TC_A_LBO0 + 16 * rot
+  i64 g7;            // global offset of tile bit 7
+  i64 ghi[TC_STEPS]; // global offsets of tile bits 8..11
+  uint32_t aoff_lo[TC_THREADS];
+  uint32_t aoff_hi[TC_STEPS];
+  uint16_t sread_lo[TC_THREADS];
+  uint16_t sread_hi[TC_STEPS];
   uint16_t scol[32];
 };
 
@@ -140,12 +146,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ i64 tile_base(i64 t, const TcGeom& geo) {
-  i64 base = 0;
-  for (int b = 0; b < geo.nrest; ++b) base |= ((t >> b) & 1) << geo.rest[b];
-  return base;
+// Global offset of tile t: its bits deposited at the rest positions, one
+// bit per lane (my_rest = position for lane < nrest, else -1), OR-reduced
+// over the warp.
+__device__ __forceinline__ i64 tile_base(i64 t, int lane, int my_rest) {
+  uint32_t lo = 0, hi = 0;
+  if (my_rest >= 0 && ((t >> lane) & 1)) {
+    const uint64_t bit = (uint64_t)1 << my_rest;
+    lo = (uint32_t)bit;
+    hi = (uint32_t)(bit >> 32);
+  }
+  lo = __reduce_or_sync(0xffffffffu, lo);
+  hi = __reduce_or_sync(0xffffffffu, hi);
+  return (i64)(((uint64_t)hi << 32) | lo);
 }
 
+// FULL: 4096-amplitude tiles (states of 12 qubits or more), no predicates.
+template <bool FULL>
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_fused5_tc(float2* __restrict__ psi, i64 ntiles, const __grid_constant__ TcGeom geo,
                 const __grid_constant__ TcGate G, int* __restrict__ err) {
@@ -153,7 +170,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t s_base = smem_u32(sm);
   const uint32_t mb = smem_u32(&mbar);
 
@@ -186,30 +203,35 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   const uint32_t tmem = tmem_base;
   constexpr uint32_t IDESC = tc_idesc(TC_M, TC_N);
   uint32_t phase = 0;
-  const int TN = 1 << geo.nbits;
-  const int nr = TN >= TC_THREADS ? TN / TC_THREADS : 1;  // steps per thread
-  const bool tval = tid < TN;                             // this thread has elements
+  const int TN = FULL ? TC_TILE : (1 << geo.nbits);
+  const int nr = FULL ? TC_STEPS : (TN >= TC_THREADS ? TN / TC_THREADS : 1);  // steps per thread
+  const bool tval = FULL || tid < TN;                                        // this thread has elements
   const int nrows = TN >> 5;
   const uint32_t aoff = geo.aoff_lo[tid];
   const uint32_t srd = geo.sread_lo[tid];
   const uint32_t a_lbo = geo.a_lbo;
+  const int my_rest = lane < geo.nrest ? geo.rest[lane] : -1;
+  const i64 toff = (i64)(tid & 127) + ((tid >> 7) ? geo.g7 : 0);
   float2* stage = (float2*)(sm + TC_OFF_AHI);
+  // epilogue: this warp's TMEM sub-partition (group rows) and column half
+  const int erow = 32 * (warp & 3) + lane;
+  const int ehalf = warp >> 2;
 
-  float2 v[32];
+  float2 v[TC_STEPS];
   i64 t = blockIdx.x;
   i64 base = 0;
   if (t < ntiles) {
-    base = tile_base(t, geo);
-    const float2* src = psi + base + tid;
+    base = tile_base(t, lane, my_rest);
+    const float2* src = psi + base + toff;
 #pragma unroll
-    for (int r = 0; r < 32; ++r)
-      if (tval && r < nr) v[r] = src[geo.ghi[r]];
+    for (int r = 0; r < TC_STEPS; ++r)
+      if (FULL || (tval && r < nr)) v[r] = src[geo.ghi[r]];
   }
   for (; t < ntiles; t += gridDim.x) {
     // registers -> A_hi / A_lo (row = group, columns 2c, 2c+1 = re, im of element c)
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
-      if (tval && r < nr) {
+    for (int r = 0; r < TC_STEPS; ++r) {
+      if (FULL || (tval && r < nr)) {
         const float2 x = v[r];
         const float2 h = make_float2(tf32_head(x.x), tf32_head(x.y));
         const uint32_t o = aoff + geo.aoff_hi[r];
@@ -247,39 +269,40 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     const i64 tn = t + gridDim.x;
     i64 nbase = 0;
     if (tn < ntiles) {
-      nbase = tile_base(tn, geo);
-      const float2* src = psi + nbase + tid;
+      nbase = tile_base(tn, lane, my_rest);
+      const float2* src = psi + nbase + toff;
 #pragma unroll
-      for (int r = 0; r < 32; ++r)
-        if (tval && r < nr) v[r] = src[geo.ghi[r]];
+      for (int r = 0; r < TC_STEPS; ++r)
+        if (FULL || (tval && r < nr)) v[r] = src[geo.ghi[r]];
     }
-    const bool ok = mbar_wait(mb, phase);
-    if (!ok) atomicExch(&abort_flag, 1);
+    // one thread waits for the MMAs; the rest park at the barrier
+    if (tid == 0 && !mbar_wait(mb, phase)) abort_flag = 1;
     __syncthreads();
     if (abort_flag) {
       // record the failure, give the in-flight MMAs one more bounded wait so
       // tensor memory is not freed under them, then leave
-      if (tid == 0) atomicExch(err, 1);
-      mbar_wait(mb, phase);
+      if (tid == 0) {
+        atomicExch(err, 1);
+        mbar_wait(mb, phase);
+      }
       break;
     }
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // TMEM lane (32*warp + lane) = row tid = this thread's group
-    float y[64];
-    const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) tmem_ld16(ta + q * 16, y + q * 16);
+    float y[32];
+    const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32 * ehalf;
+    tmem_ld16(ta, y);
+    tmem_ld16(ta + 16, y + 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    if (tid < nrows) {
+    if (FULL || erow < nrows) {
 #pragma unroll
-      for (int c = 0; c < 32; ++c) stage[tid ^ geo.scol[c]] = make_float2(y[2 * c], y[2 * c + 1]);
+      for (int c = 0; c < 16; ++c) stage[erow ^ geo.scol[16 * ehalf + c]] = make_float2(y[2 * c], y[2 * c + 1]);
     }
     __syncthreads();
-    float2* dst = psi + base + tid;
+    float2* dst = psi + base + toff;
 #pragma unroll
-    for (int r = 0; r < 32; ++r)
-      if (tval && r < nr) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
+    for (int r = 0; r < TC_STEPS; ++r)
+      if (FULL || (tval && r < nr)) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     base = nbase;
@@ -322,7 +345,7 @@ void make_geom(int n, const std::vector<int>& tbits, TcGeom* geo, int cbit[5]) {
   // with t4 = 0 the column is fixed and 2 wavefronts are the minimum).
   int t4 = 0;
   for (int b : tbits) t4 += b < 4;
-  const uint32_t rot = t4 >= 4 ? 1 : t4 == 3 ? 2 : t4 == 2 ? 4 : 1;
+  const uint32_t rot = t4 == 3 ? 2 : t4 == 2 ? 4 : 1;
   geo->a_lbo = TC_A_LBO0 + 16 * rot;
   const int gsh = 4 - t4;
   auto scol = [&](uint32_t c) { return (uint32_t)((c << 7) ^ ((c << gsh) & 15u)); };
@@ -338,25 +361,35 @@ void make_geom(int n, const std::vector<int>& tbits, TcGeom* geo, int cbit[5]) {
       else *col |= 1u << colbit[b];
     }
   };
-  for (int v = 0; v < 128; ++v) {
+  for (int v = 0; v < TC_THREADS; ++v) {
     i64 dep;
     uint32_t row, col;
-    split(v, 0, 7, &dep, &row, &col);
+    split(v, 0, 8, &dep, &row, &col);
     geo->aoff_lo[v] = core_off(row, 2 * col, geo->a_lbo, TC_A_SBO);
     geo->sread_lo[v] = (uint16_t)(row ^ scol(col));
   }
-  for (int r = 0; r < 32; ++r) {
+  geo->g7 = nb > 7 ? (i64)1 << pos[7] : 0;
+  for (int r = 0; r < TC_STEPS; ++r) {
     i64 dep;
     uint32_t row, col;
-    split(r, 7, 5, &dep, &row, &col);
+    split(r, 8, 4, &dep, &row, &col);
     geo->ghi[r] = dep;
     geo->aoff_hi[r] = core_off(row, 2 * col, geo->a_lbo, TC_A_SBO);
     geo->sread_hi[r] = (uint16_t)(row ^ scol(col));
-    geo->scol[r] = (uint16_t)scol((uint32_t)r);
   }
+  for (int c = 0; c < 32; ++c) geo->scol[c] = (uint16_t)scol((uint32_t)c);
   geo->nrest = 0;
   for (int b = 0; b < n; ++b)
     if (std::find(pos.begin(), pos.end(), b) == pos.end()) geo->rest[geo->nrest++] = b;
+}
+
+template <bool FULL>
+void set_tc_smem_attr() {
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(k_fused5_tc<FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    done = true;
+  }
 }
 }  // namespace
 
@@ -385,14 +418,15 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
       G->ur[r][c] = (float)u.real();
       G->ui[r][c] = (float)u.imag();
     }
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_fused5_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    attr = true;
-  }
   const i64 ntiles = (i64)1 << (n - geo->nbits);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
-  k_fused5_tc<<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
+  if (geo->nbits == 12) {
+    set_tc_smem_attr<true>();
+    k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
+  } else {
+    set_tc_smem_attr<false>();
+    k_fused5_tc<false><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
+  }
   delete G;
   delete geo;
   QGB_LAUNCH_CHECK("k_fused5_tc");
