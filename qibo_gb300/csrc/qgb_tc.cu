@@ -383,6 +383,16 @@ void make_geom(int n, const std::vector<int>& tbits, TcGeom* geo, int cbit[5]) {
     if (std::find(pos.begin(), pos.end(), b) == pos.end()) geo->rest[geo->nrest++] = b;
 }
 
+// Permuted block matrix U'[r'][c'] = U[idx[r']][idx[c']]: idx[c'] is the
+// block index whose bit (4 - jt) is bit cbit[jt] of c'.
+void block_perm(const int cbit[5], int idx[32]) {
+  for (int c = 0; c < 32; ++c) {
+    idx[c] = 0;
+    for (int jt = 0; jt < 5; ++jt)
+      if ((c >> cbit[jt]) & 1) idx[c] |= 1 << (4 - jt);
+  }
+}
+
 template <bool FULL>
 void set_tc_smem_attr() {
   static bool done = false;
@@ -403,14 +413,8 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   TcGeom* geo = new TcGeom();
   int cbit[5];
   make_geom(n, g.tbits, geo, cbit);
-  // permuted block matrix U'[r'][c'] = U[i(r')][i(c')], i(c') the block
-  // index whose bit (4 - jt) is bit cbit[jt] of c'
   int idx[32];
-  for (int c = 0; c < 32; ++c) {
-    idx[c] = 0;
-    for (int jt = 0; jt < 5; ++jt)
-      if ((c >> cbit[jt]) & 1) idx[c] |= 1 << (4 - jt);
-  }
+  block_perm(cbit, idx);
   TcGate* G = new TcGate();
   for (int r = 0; r < 32; ++r)
     for (int c = 0; c < 32; ++c) {

@@ -1,0 +1,175 @@
+// Host-side check of the tensor-core block kernel's index tables.
+//
+// Includes qgb_tc.cu and replays k_fused5_tc's data movement on the CPU with
+// the tables make_geom builds: the coalesced load (thread t, step r -> global
+// offset), the A operand layout (decoded back to (group row, column)), the
+// permuted block product in FP64, the staging slots of the epilogue and the
+// coalesced store.  For n = 5..16 and random, lowest and highest block-qubit
+// placements it checks that every amplitude is read and written exactly
+// once, that every shared-memory offset lies inside its buffer and is used
+// once, and that the result equals the block applied directly.  It also
+// counts shared-memory wavefronts per warp access (8-byte accesses, one
+// wavefront per half-warp without conflicts) and fails if any pattern needs
+// more than the layout promises: 2 per warp for the staging writes and
+// reads, 2 for A writes of blocks with a qubit on index bits 0..3, else 4.
+// No kernel is launched.
+#include <complex>
+#include <cstdio>
+#include <map>
+#include <random>
+#include <set>
+
+#include "qgb_tc.cu"
+
+typedef std::complex<double> cd;
+
+static i64 host_tile_base(i64 t, const TcGeom& geo) {
+  i64 base = 0;
+  for (int b = 0; b < geo.nrest; ++b) base |= ((t >> b) & 1) << geo.rest[b];
+  return base;
+}
+
+// wavefronts of one warp of 8-byte shared-memory accesses (byte offsets)
+static int wavefronts(const uint32_t* off) {
+  int total = 0;
+  for (int h = 0; h < 2; ++h) {
+    std::map<int, std::set<uint32_t>> bank;
+    for (int l = 16 * h; l < 16 * h + 16; ++l) {
+      bank[(off[l] / 4) % 32].insert(off[l] / 4);
+      bank[(off[l] / 4 + 1) % 32].insert(off[l] / 4 + 1);
+    }
+    int m = 0;
+    for (auto& kv : bank) m = std::max<int>(m, (int)kv.second.size());
+    total += m;
+  }
+  return total;
+}
+
+int main() {
+  std::mt19937_64 rng(5);
+  std::normal_distribution<double> nd;
+  int fails = 0, cases = 0, bank_fails = 0;
+  for (int n = 5; n <= 16; ++n) {
+    for (int trial = 0; trial < 24; ++trial) {
+      std::vector<int> all(n);
+      for (int i = 0; i < n; ++i) all[i] = i;
+      std::shuffle(all.begin(), all.end(), rng);
+      std::vector<int> tb(all.begin(), all.begin() + 5);
+      if (trial == 0) tb = {4, 3, 2, 1, 0};
+      if (trial == 1) tb = {n - 1, n - 2, n - 3, n - 4, n - 5};
+      if (trial == 2) tb = {0, 1, 2, 3, 4};
+      std::vector<zd> U(1024);
+      for (auto& c : U) c = zd(nd(rng), nd(rng));
+      TcGeom* geo = new TcGeom();
+      int cbit[5], idx[32];
+      make_geom(n, tb, geo, cbit);
+      block_perm(cbit, idx);
+      int t4 = 0;
+      for (int b : tb) t4 += b < 4;
+      const i64 N = (i64)1 << n;
+      std::vector<cd> psi(N), out(N, cd(0, 0)), ref(N);
+      for (auto& x : psi) x = cd(nd(rng), nd(rng));
+      for (i64 i = 0; i < N; ++i) {  // the block applied directly
+        int bi = 0;
+        for (int jt = 0; jt < 5; ++jt) bi |= (int)((i >> tb[jt]) & 1) << (4 - jt);
+        if (bi) continue;
+        i64 id[32];
+        for (int b = 0; b < 32; ++b) {
+          id[b] = i;
+          for (int jt = 0; jt < 5; ++jt)
+            if ((b >> (4 - jt)) & 1) id[b] |= (i64)1 << tb[jt];
+        }
+        for (int r = 0; r < 32; ++r) {
+          cd acc = 0;
+          for (int c = 0; c < 32; ++c) acc += cd(U[r * 32 + c].real(), U[r * 32 + c].imag()) * psi[id[c]];
+          ref[id[r]] = acc;
+        }
+      }
+      const int TN = 1 << geo->nbits;
+      const int nr = TN >= TC_THREADS ? TN / TC_THREADS : 1;
+      const int nrows = TN >> 5;
+      const i64 ntiles = (i64)1 << (n - geo->nbits);
+      std::map<uint32_t, std::pair<int, int>> dec;  // A byte offset -> (row, k)
+      for (int row = 0; row < TC_M; ++row)
+        for (int k = 0; k < TC_K; ++k) dec[core_off(row, k, geo->a_lbo, TC_A_SBO)] = {row, k};
+      std::vector<int> seen(N, 0), wrote(N, 0);
+      bool bad = false;
+      for (i64 t = 0; t < ntiles; ++t) {
+        const i64 base = host_tile_base(t, *geo);
+        std::vector<double> A(TC_M * TC_K, 0.0);
+        std::set<uint32_t> used;
+        for (int r = 0; r < TC_STEPS; ++r) {
+          for (int tid = 0; tid < TC_THREADS; ++tid) {
+            if (!(tid < TN && r < nr)) continue;
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            if (gi < 0 || gi >= N) { bad = true; continue; }
+            seen[gi]++;
+            const uint32_t o = geo->aoff_lo[tid] + geo->aoff_hi[r];
+            if (o + 8 > (uint32_t)TC_A_BYTES || !dec.count(o) || used.count(o)) { bad = true; continue; }
+            used.insert(o);
+            const auto rk = dec[o];
+            A[rk.first * TC_K + rk.second] = psi[gi].real();
+            A[rk.first * TC_K + rk.second + 1] = psi[gi].imag();
+          }
+          if (t == 0 && TN == TC_TILE)
+            for (int w = 0; w < TC_THREADS / 32; ++w) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = geo->aoff_lo[32 * w + l] + geo->aoff_hi[r];
+              if (wavefronts(off) > (t4 >= 1 ? 2 : 4)) bank_fails++;
+            }
+        }
+        std::vector<cd> stage(TC_TILE, cd(1e300, 0));
+        for (int row = 0; row < nrows; ++row)
+          for (int c = 0; c < 32; ++c) {
+            cd acc = 0;
+            for (int k = 0; k < 32; ++k) {
+              const zd u = U[idx[c] * 32 + idx[k]];
+              acc += cd(u.real(), u.imag()) * cd(A[row * TC_K + 2 * k], A[row * TC_K + 2 * k + 1]);
+            }
+            const uint32_t si = (uint32_t)row ^ geo->scol[c];
+            if (si >= (uint32_t)TC_TILE) { bad = true; continue; }
+            stage[si] = acc;
+          }
+        if (t == 0 && TN == TC_TILE)
+          for (int w = 0; w < 4; ++w)
+            for (int c = 0; c < 32; ++c) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = 8 * ((uint32_t)(32 * w + l) ^ geo->scol[c]);
+              if (wavefronts(off) > 2) bank_fails++;
+            }
+        for (int r = 0; r < TC_STEPS; ++r) {
+          for (int tid = 0; tid < TC_THREADS; ++tid) {
+            if (!(tid < TN && r < nr)) continue;
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            if (gi < 0 || gi >= N) { bad = true; continue; }
+            const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
+            if (si >= (uint32_t)TC_TILE) { bad = true; continue; }
+            wrote[gi]++;
+            out[gi] = stage[si];
+          }
+          if (t == 0 && TN == TC_TILE)
+            for (int w = 0; w < TC_THREADS / 32; ++w) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = 8 * ((uint32_t)geo->sread_lo[32 * w + l] ^ geo->sread_hi[r]);
+              if (wavefronts(off) > 2) bank_fails++;
+            }
+        }
+      }
+      double err = 0, nrm = 0;
+      for (i64 i = 0; i < N; ++i) {
+        if (seen[i] != 1 || wrote[i] != 1) bad = true;
+        err = std::max(err, std::abs(out[i] - ref[i]));
+        nrm = std::max(nrm, std::abs(ref[i]));
+      }
+      ++cases;
+      if (bad || err > 1e-9 * nrm) {
+        ++fails;
+        printf("FAIL n=%d block bits %d,%d,%d,%d,%d err=%g bad=%d\n", n, tb[0], tb[1], tb[2], tb[3], tb[4], err,
+               (int)bad);
+      }
+      delete geo;
+    }
+  }
+  printf("cases %d index failures %d bank-pattern failures %d\n", cases, fails, bank_fails);
+  return (fails || bank_fails) ? 1 : 0;
+}
