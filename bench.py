@@ -271,10 +271,10 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
         qs = _lib.int_array(blk[0])
         mat = np.ascontiguousarray(np.asarray(blk[2], dtype=np.complex128)).view(np.float64).ravel()
         mp = mat.ctypes.data_as(_lib.dp)
-        check(lib.qgb_apply_fused5_tc(st64.ptr, n, qs, mp, rt.stream))
+        check(lib.qgb_apply_fused5_tc(st64.ptr, n, st64.code, qs, mp, rt.stream))
         ev.start(rt.stream)
         for _ in range(10):
-            check(lib.qgb_apply_fused5_tc(st64.ptr, n, qs, mp, rt.stream))
+            check(lib.qgb_apply_fused5_tc(st64.ptr, n, st64.code, qs, mp, rt.stream))
         tc_ms = ev.stop_ms(rt.stream) / 10
         tc_gbs = 2 * 2**n * 8 / (tc_ms * 1e-3) / 1e9
     tc_timeout = C.c_int(0)
@@ -487,10 +487,12 @@ def run_serving(args):
 
 
 def run_tc5(args):
-    """k_fused5_tc alone: a random 5-qubit unitary applied to a complex64
-    state of ``--nqubits`` qubits (default 30, 8.6 GB; inputs >> L2), one
-    launch per step, for three placements of the block qubits (lowest index
-    bits, highest, spread).  Algorithmic bytes per launch: 2 * 2^n * 8."""
+    """The tensor-core block kernels alone: a random 5-qubit unitary applied to
+    a state of ``--nqubits`` qubits (default 30; 8.6 GB in complex64, 17.2 GB
+    in complex128, inputs >> L2), one launch per step, for three placements
+    of the block qubits (lowest index bits, highest, spread), in complex64
+    (k_fused5_tc, 3xTF32) and complex128 (k_fused5_oz, Ozaki scheme on BF16).
+    Algorithmic bytes per launch: 2 * 2^n * S."""
     from qibo_gb300 import _lib
     from qibo_gb300._lib import check
     from qibo_gb300.backend import GB300Backend
@@ -499,8 +501,6 @@ def run_tc5(args):
     n = args.nqubits
     b = GB300Backend("complex64")
     rt, lib = b.rt, b.rt.lib
-    st = DeviceState(n, "complex64")
-    check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
     rng = np.random.default_rng(5)
     z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
     u, _ = np.linalg.qr(z)
@@ -508,23 +508,30 @@ def run_tc5(args):
     mp = mat.ctypes.data_as(_lib.dp)
     peak = measured_peaks().get("hbm_gbs", 6800.0)
     ev = Events(lib)
-    nbytes = 2 * 2**n * 8
     out = {}
-    for name, qs in (("high_bits", [0, 1, 2, 3, 4]), ("low_bits", [n - 1, n - 2, n - 3, n - 4, n - 5]),
-                     ("spread", [1, n // 3, n // 2, n - 3, n - 1])):
-        qa = _lib.int_array(qs)
-        for _ in range(args.warmup):
-            check(lib.qgb_apply_fused5_tc(st.ptr, n, qa, mp, rt.stream))
-        ev.start(rt.stream)
-        for _ in range(args.steps):
-            check(lib.qgb_apply_fused5_tc(st.ptr, n, qa, mp, rt.stream))
-        ms = ev.stop_ms(rt.stream) / args.steps
-        gbs = nbytes / (ms * 1e-3) / 1e9
-        out[name] = {"qubits": qs, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
-                     "tensor_tflops_3xtf32": 3 * 2 * 64 * 64 * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
+    for dtype, kernel, S, flops in (("complex64", "k_fused5_tc", 8, 3 * 2 * 64 * 64),
+                                     ("complex128", "k_fused5_oz", 16, 26 * 2 * 64 * 64)):
+        st = DeviceState(n, dtype)
+        check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+        nbytes = 2 * 2**n * S
+        res = {"kernel": kernel, "bytes_per_launch": nbytes}
+        for name, qs in (("high_bits", [0, 1, 2, 3, 4]), ("low_bits", [n - 1, n - 2, n - 3, n - 4, n - 5]),
+                         ("spread", [1, n // 3, n // 2, n - 3, n - 1])):
+            qa = _lib.int_array(qs)
+            for _ in range(args.warmup):
+                check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, qa, mp, rt.stream))
+            ev.start(rt.stream)
+            for _ in range(args.steps):
+                check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, qa, mp, rt.stream))
+            ms = ev.stop_ms(rt.stream) / args.steps
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            res[name] = {"qubits": qs, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
+                         "tensor_tflops": flops * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
+        out[dtype] = res
+        del st
     flag = C.c_int(0)
     check(lib.qgb_tc_status(C.byref(flag)))
-    print(json.dumps({"workload": f"k_fused5_tc, complex64 n={n}, random 5-qubit unitary", "bytes_per_launch": nbytes,
+    print(json.dumps({"workload": f"fused 5-qubit block kernels, n={n}, random 5-qubit unitary",
                       "hbm_peak_gbs": peak, "tc_wait_timeouts": flag.value, **out}))
 
 

@@ -104,9 +104,10 @@ int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1,
  * Complex128 passes compute in double-float (two FP32 words per double,
  * about 48 significant bits) on the FP32 pipe unless
  * ``flags & QGB_PLAN_STRICT_FP64`` asks for IEEE FP64 arithmetic; the
- * gate-by-gate path always computes complex128 in IEEE FP64.  For complex64,
- * uncontrolled 5-qubit dense blocks (fused gates) run on the tensor cores
- * (qgb_apply_fused5_tc) unless ``flags & QGB_PLAN_NO_TC``. */
+ * gate-by-gate path always computes complex128 in IEEE FP64.  With
+ * QGB_PLAN_BLOCKED, uncontrolled 5-qubit dense blocks (fused gates) run on
+ * the tensor cores (qgb_apply_fused5_tc; complex128 from 12 qubits) unless
+ * ``flags & QGB_PLAN_NO_TC``. */
 typedef struct qgb_op {
     int32_t k;              /* number of gate qubits (<= 5) */
     int32_t ncontrols;      /* number of controls (<= 8) */
@@ -116,7 +117,7 @@ typedef struct qgb_op {
 } qgb_op;
 #define QGB_PLAN_BLOCKED 1
 #define QGB_PLAN_STRICT_FP64 2
-#define QGB_PLAN_NO_TC 8       /* complex64: fused 5-qubit blocks on CUDA cores instead of tensor cores */
+#define QGB_PLAN_NO_TC 8       /* fused 5-qubit blocks in shared-memory passes instead of on the tensor cores */
 int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, int flags, void* stream);
 /* Number of state passes QGB_PLAN_BLOCKED would launch for this gate list
@@ -125,13 +126,18 @@ int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int nops, const d
 
 /* A fused 5-qubit block (FusedGate, gates/special.py:28-153, applied by
  * Backend.apply_gate with Backend.matrix_fused, backends/abstract.py:
- * 2680-2717) on a complex64 state, computed on the tensor cores: 128 groups
- * of 32 amplitudes per tcgen05 MMA tile, 3xTF32 split (A_hi*B_hi + A_hi*B_lo
- * + A_lo*B_hi) with FP32 accumulation in tensor memory.  ``matrix`` as for
- * qgb_apply_gate (32x32, qubits[0] most significant). */
-int qgb_apply_fused5_tc(void* state, int nqubits, const int* qubits, const double* matrix, void* stream);
-/* *timed_out = 1 if a tensor-core launch gave up waiting for its MMAs (the
- * launch then stopped early and its output is invalid).  Synchronising. */
+ * 2680-2717) computed on the tensor cores, 128 groups of 32 amplitudes per
+ * tcgen05 MMA tile.  complex64 (nqubits >= 5): 3xTF32 split (A_hi*B_hi +
+ * A_hi*B_lo + A_lo*B_hi) with FP32 accumulation in tensor memory.
+ * complex128 (nqubits >= 12): Ozaki scheme on the BF16 tensor cores, six
+ * 8-bit digits per value in 47-bit fixed point, six exact FP32 level
+ * accumulators, combined into IEEE doubles (error per output about 2^-45 of
+ * the tile scale).  ``matrix`` as for qgb_apply_gate (32x32, qubits[0] most
+ * significant).  QGB_ERR_UNSUPPORTED below the qubit minimum. */
+int qgb_apply_fused5_tc(void* state, int nqubits, int dtype, const int* qubits, const double* matrix, void* stream);
+/* *timed_out = 1 if a tensor-core launch since the previous call gave up
+ * waiting for its MMAs (that launch stopped early and its output is
+ * invalid); clears the flag.  Synchronising. */
 int qgb_tc_status(int* timed_out);
 
 /* ---- measurement: Backend.calculate_probabilities (:2734-2758,

@@ -73,7 +73,7 @@ SIGNATURES = {
     "qgb_apply_swap": (i32, [vp, i32, i32, i32, i32, ip, i32, vp]),
     "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),
     "qgb_plan_passes": (i32, [i32, i32, C.POINTER(QgbOp), i32, dp, ip]),
-    "qgb_apply_fused5_tc": (i32, [vp, i32, ip, dp, vp]),
+    "qgb_apply_fused5_tc": (i32, [vp, i32, i32, ip, dp, vp]),
     "qgb_tc_status": (i32, [ip]),
     "qgb_probs_scratch_bytes": (sz, [i32, i32]),
     "qgb_probabilities": (i32, [vp, i32, i32, ip, i32, vp, vp, vp]),

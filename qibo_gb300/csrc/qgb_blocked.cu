@@ -234,6 +234,7 @@ int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vect
 }  // namespace
 
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc.cu
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc128.cu
 
 namespace {
 bool is_tc_block(const GateOp& g) { return g.kind == GK_DENSE && g.tbits.size() == 5 && g.cbits.empty(); }
@@ -258,9 +259,11 @@ int run_segment(void* state, int nqubits, int dtype, const std::vector<GateOp>& 
 }
 }  // namespace
 
-// Blocked execution.  For complex64, fused 5-qubit blocks (uncontrolled dense
-// 32x32) run on the tensor cores (qgb_tc.cu), one pass each; the gates
-// between two such blocks are planned into shared-memory passes.
+// Blocked execution.  Fused 5-qubit blocks (uncontrolled dense 32x32) run on
+// the tensor cores, one pass each: complex64 in 3xTF32 (qgb_tc.cu), complex128
+// from 12 qubits in the Ozaki scheme on BF16 (qgb_tc128.cu; not under
+// strict FP64, which keeps IEEE arithmetic).  The gates between two such
+// blocks are planned into shared-memory passes.
 int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs,
                     bool strict_fp64, bool use_tc, cudaStream_t s) {
   std::vector<GateOp> g(nops);
@@ -269,7 +272,8 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
                           coefs + ops[i].coef_offset, &g[i], "qgb_apply_circuit");
     if (st) return st;
   }
-  if (!(use_tc && dtype == QGB_C64)) return run_segment(state, nqubits, dtype, g, strict_fp64, s);
+  const bool tc_ok = use_tc && (dtype == QGB_C64 || (dtype == QGB_C128 && nqubits >= 12 && !strict_fp64));
+  if (!tc_ok) return run_segment(state, nqubits, dtype, g, strict_fp64, s);
   std::vector<GateOp> seg;
   for (int i = 0; i <= nops; ++i) {
     const bool tc = i < nops && is_tc_block(g[i]);
@@ -280,7 +284,8 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
         seg.clear();
       }
       if (tc) {
-        int st = qgb_launch_fused5_tc(state, nqubits, g[i], s);
+        int st = dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, g[i], s)
+                                   : qgb_launch_fused5_tc(state, nqubits, g[i], s);
         if (st) return st;
       }
     } else {

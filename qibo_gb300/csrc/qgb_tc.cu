@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "qgb_plan.h"
+#include "qgb_tcgen05.cuh"
 
 #define TC_M 128
 #define TC_N 64
@@ -63,7 +64,6 @@
 #define TC_OFF_BHI (TC_OFF_ALO + TC_A_BYTES)
 #define TC_OFF_BLO (TC_OFF_BHI + TC_B_BYTES)
 #define TC_SMEM (TC_OFF_BLO + TC_B_BYTES)  // 108 544
-#define TC_SPIN_LIMIT (1u << 26)
 
 static_assert(TC_TILE * 8 <= TC_A_BYTES, "staging buffer must fit in A_hi");
 static_assert(TC_A_BYTES % 16 == 0 && TC_B_BYTES % 16 == 0, "operand regions 16-byte aligned");
@@ -103,63 +103,12 @@ __host__ __device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t k, 
   return (k >> 2) * lbo + (row >> 3) * sbo + (row & 7) * 16 + (k & 3) * 4;
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for this architecture
-  // base offset 0, absolute LBO mode 0, layout type 0 (no swizzle)
-  return d;
-}
-
 // kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major, N, M
 __host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ float tf32_head(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
-
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-  for (uint32_t it = 0; it < TC_SPIN_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// Global offset of tile t: its bits deposited at the rest positions, one
-// bit per lane (my_rest = position for lane < nrest, else -1), OR-reduced
-// over the warp.
-__device__ __forceinline__ i64 tile_base(i64 t, int lane, int my_rest) {
-  uint32_t lo = 0, hi = 0;
-  if (my_rest >= 0 && ((t >> lane) & 1)) {
-    const uint64_t bit = (uint64_t)1 << my_rest;
-    lo = (uint32_t)bit;
-    hi = (uint32_t)(bit >> 32);
-  }
-  lo = __reduce_or_sync(0xffffffffu, lo);
-  hi = __reduce_or_sync(0xffffffffu, hi);
-  return (i64)(((uint64_t)hi << 32) | lo);
-}
 
 // FULL: 4096-amplitude tiles (states of 12 qubits or more), no predicates.
 template <bool FULL>
@@ -313,6 +262,21 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 
 namespace {
 int* g_tc_err = nullptr;
+}  // namespace
+
+// Device flag the tensor-core kernels set when a bounded mbarrier wait gives
+// up; allocated and zeroed on first use, cleared by qgb_tc_status.
+int* qgb_tc_err_flag() {
+  if (!g_tc_err) {
+    if (cudaMalloc(&g_tc_err, sizeof(int)) != cudaSuccess || cudaMemset(g_tc_err, 0, sizeof(int)) != cudaSuccess) {
+      qgb_set_error("tensor-core error flag: %s", cudaGetErrorString(cudaGetLastError()));
+      g_tc_err = nullptr;
+    }
+  }
+  return g_tc_err;
+}
+
+namespace {
 
 // Tile geometry of a block on target bits tbits (matrix order: tbits[0] is
 // the most significant bit of the block index) of an n-qubit state.  Column
@@ -403,13 +367,15 @@ void set_tc_smem_attr() {
 }
 }  // namespace
 
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc128.cu
+
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   if (g.tbits.size() != 5 || !g.cbits.empty() || n < 5) {
     qgb_set_error("qgb_apply_fused5_tc: needs an uncontrolled 5-qubit dense block");
     return QGB_ERR_INVALID;
   }
-  if (!g_tc_err) QGB_TRY_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
-  QGB_TRY_CUDA(cudaMemsetAsync(g_tc_err, 0, sizeof(int), s));
+  int* err = qgb_tc_err_flag();
+  if (!err) return QGB_ERR_CUDA;
   TcGeom* geo = new TcGeom();
   int cbit[5];
   make_geom(n, g.tbits, geo, cbit);
@@ -426,10 +392,10 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
   if (geo->nbits == 12) {
     set_tc_smem_attr<true>();
-    k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
+    k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
   } else {
     set_tc_smem_attr<false>();
-    k_fused5_tc<false><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, g_tc_err);
+    k_fused5_tc<false><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
   }
   delete G;
   delete geo;
@@ -439,10 +405,17 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
 
 extern "C" {
 
-int qgb_apply_fused5_tc(void* state, int nqubits, const int* qubits, const double* matrix, void* stream) {
-  if (!state || !qubits || !matrix || nqubits < 5 || nqubits > QGB_MAXQ) {
-    qgb_set_error("qgb_apply_fused5_tc: bad arguments (complex64 state of at least 5 qubits)");
+int qgb_apply_fused5_tc(void* state, int nqubits, int dtype, const int* qubits, const double* matrix,
+                        void* stream) {
+  const int nmin = dtype == QGB_C128 ? 12 : 5;
+  if (!state || !qubits || !matrix || (dtype != QGB_C64 && dtype != QGB_C128) || nqubits > QGB_MAXQ) {
+    qgb_set_error("qgb_apply_fused5_tc: bad arguments");
     return QGB_ERR_INVALID;
+  }
+  if (nqubits < nmin) {
+    qgb_set_error("qgb_apply_fused5_tc: %s needs at least %d qubits (got %d)", dtype == QGB_C128 ? "complex128" : "complex64",
+                  nmin, nqubits);
+    return QGB_ERR_UNSUPPORTED;
   }
   GateOp g;
   int st = qgb_classify(nqubits, nullptr, 0, qubits, 5, nullptr, &g, "qgb_apply_fused5_tc");  // range/repeat checks
@@ -452,7 +425,8 @@ int qgb_apply_fused5_tc(void* state, int nqubits, const int* qubits, const doubl
   for (int j = 0; j < 5; ++j) g.tbits.push_back(nqubits - 1 - qubits[j]);
   g.coef.resize(1024);
   for (int i = 0; i < 1024; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
-  return qgb_launch_fused5_tc(state, nqubits, g, (cudaStream_t)stream);
+  return dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, g, (cudaStream_t)stream)
+                           : qgb_launch_fused5_tc(state, nqubits, g, (cudaStream_t)stream);
 }
 
 int qgb_tc_status(int* timed_out) {
@@ -461,7 +435,10 @@ int qgb_tc_status(int* timed_out) {
     return QGB_ERR_INVALID;
   }
   *timed_out = 0;
-  if (g_tc_err) QGB_TRY_CUDA(cudaMemcpy(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (g_tc_err) {
+    QGB_TRY_CUDA(cudaMemcpy(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    QGB_TRY_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
+  }
   return QGB_OK;
 }
 

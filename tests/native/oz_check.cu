@@ -1,0 +1,235 @@
+// Host-side check of the complex128 tensor-core block kernel (Ozaki scheme).
+//
+// Includes qgb_tc128.cu and replays k_fused5_oz on the CPU with the tables
+// make_oz_geom builds and the same digit / combine functions the kernel
+// calls: tile scale, balanced digits into the bf16 A slices (decoded back
+// from their byte offsets), the stacked B slices, the level accumulators as
+// exact integer sums (checked below 2^24, hence exact in FP32), the
+// combination into doubles, the staging slots and the stores.  Compares with
+// the block applied in FP64 for n = 12..15 and random, lowest and highest
+// block placements, plus states with a wide dynamic range: every output must
+// be within 2^-41 of 2^(E + F) (E, F the exponents of its tile and gate-row
+// scales, the worst-case bound of the fixed-point rounding over K = 64), and
+// the largest error over a Gaussian state within 1e-13 of its largest output.
+// Also counts shared-memory wavefronts of the A writes (4-byte) and of the
+// staging writes and reads (16-byte).
+// No kernel is launched.
+#include <complex>
+#include <cstdio>
+#include <map>
+#include <random>
+#include <set>
+
+#include "qgb_tc128.cu"
+
+typedef std::complex<double> cd;
+
+static i64 host_tile_base(i64 t, const OzGeom& geo) {
+  i64 base = 0;
+  for (int b = 0; b < geo.nrest; ++b) base |= ((t >> b) & 1) << geo.rest[b];
+  return base;
+}
+
+// wavefronts of one warp access: `width` bytes per lane at byte offsets off[32]
+static int wavefronts(const uint32_t* off, int width) {
+  const int group = 128 / width;  // lanes served per wavefront without conflicts
+  int total = 0;
+  for (int g0 = 0; g0 < 32; g0 += group) {
+    std::map<int, std::set<uint32_t>> bank;
+    for (int l = g0; l < g0 + group; ++l)
+      for (int w = 0; w < width / 4; ++w) bank[(off[l] / 4 + w) % 32].insert(off[l] / 4 + w);
+    int m = 0;
+    for (auto& kv : bank) m = std::max<int>(m, (int)kv.second.size());
+    total += m;
+  }
+  return total;
+}
+
+int main() {
+  std::mt19937_64 rng(11);
+  std::normal_distribution<double> nd;
+  int fails = 0, cases = 0, bank_fails = 0, exact_fails = 0;
+  double worst = 0;
+  for (int n = 12; n <= 15; ++n) {
+    for (int trial = 0; trial < 16; ++trial) {
+      std::vector<int> all(n);
+      for (int i = 0; i < n; ++i) all[i] = i;
+      std::shuffle(all.begin(), all.end(), rng);
+      std::vector<int> tb(all.begin(), all.begin() + 5);
+      if (trial == 0) tb = {4, 3, 2, 1, 0};
+      if (trial == 1) tb = {n - 1, n - 2, n - 3, n - 4, n - 5};
+      if (trial == 2) tb = {2, 0, 1, 9, 3};
+      GateOp g;
+      g.kind = GK_DENSE;
+      g.tbits = tb;
+      g.coef.resize(1024);
+      for (auto& c : g.coef) c = zd(nd(rng), nd(rng)) * 0.2;
+      OzGeom* geo = new OzGeom();
+      OzGate* G = new OzGate();
+      int cbit[5];
+      make_oz_geom(n, tb, geo, cbit);
+      make_oz_gate(g, cbit, G);
+      int t5 = 0;
+      for (int b : tb) t5 += b < 5;
+      const i64 N = (i64)1 << n;
+      std::vector<cd> psi(N), out(N, cd(0, 0)), ref(N);
+      std::vector<double> bound(N, 0.0);
+      const bool wide = trial % 4 == 3;  // amplitudes over ~2^-40 .. 1
+      for (auto& x : psi) {
+        x = cd(nd(rng), nd(rng));
+        if (wide) x *= std::ldexp(1.0, -(int)(rng() % 40));
+      }
+      for (i64 i = 0; i < N; ++i) {  // the block applied directly
+        int bi = 0;
+        for (int jt = 0; jt < 5; ++jt) bi |= (int)((i >> tb[jt]) & 1) << (4 - jt);
+        if (bi) continue;
+        i64 id[32];
+        for (int b = 0; b < 32; ++b) {
+          id[b] = i;
+          for (int jt = 0; jt < 5; ++jt)
+            if ((b >> (4 - jt)) & 1) id[b] |= (i64)1 << tb[jt];
+        }
+        for (int r = 0; r < 32; ++r) {
+          cd acc = 0;
+          for (int c = 0; c < 32; ++c) acc += cd(g.coef[r * 32 + c].real(), g.coef[r * 32 + c].imag()) * psi[id[c]];
+          ref[id[r]] = acc;
+        }
+      }
+      // stacked B slices as integers: Bd[j][n][k]
+      static int Bd[OZ_NSLICE][64][64];
+      for (int nn = 0; nn < 64; ++nn)
+        for (int k = 0; k < 64; ++k) {
+          const int r = nn >> 1, c = k >> 1;
+          double v;
+          if ((nn & 1) == 0) v = (k & 1) == 0 ? G->ur[r][c] : -G->ui[r][c];
+          else v = (k & 1) == 0 ? G->ui[r][c] : G->ur[r][c];
+          int d[OZ_NSLICE];
+          oz_digits(v, G->fexp[r], d);
+          for (int j = 0; j < OZ_NSLICE; ++j) {
+            Bd[j][nn][k] = d[j];
+            if (oz_boff(64 * j + nn, k) + 2 > 8 * OZ_B_LBO) exact_fails++;
+          }
+        }
+      std::map<uint32_t, std::pair<int, int>> dec;  // A slice byte offset of (row, c) pair
+      for (int row = 0; row < 128; ++row)
+        for (int c = 0; c < 32; ++c)
+          dec[(c >> 2) * geo->a_lbo + (row >> 3) * OZ_A_SBO + (row & 7) * 16 + (c & 3) * 4] = {row, c};
+      std::vector<int> seen(N, 0), wrote(N, 0);
+      bool bad = false;
+      const i64 ntiles = (i64)1 << (n - 12);
+      for (i64 t = 0; t < ntiles; ++t) {
+        const i64 base = host_tile_base(t, *geo);
+        int exm = 0;
+        for (int r = 0; r < OZ_STEPS; ++r)
+          for (int tid = 0; tid < OZ_THREADS; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            if (gi < 0 || gi >= N) { bad = true; continue; }
+            exm = std::max(exm, (int)((oz_dbits(psi[gi].real()) >> 52) & 0x7FF));
+            exm = std::max(exm, (int)((oz_dbits(psi[gi].imag()) >> 52) & 0x7FF));
+          }
+        static int Ad[OZ_NSLICE][128][64];
+        std::set<uint32_t> used;
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          for (int tid = 0; tid < OZ_THREADS; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            if (gi < 0 || gi >= N) { bad = true; continue; }
+            seen[gi]++;
+            const uint32_t o = geo->aoff_lo[tid] + geo->aoff_hi[r];
+            if (o + 4 > (uint32_t)OZ_A_SLICE || !dec.count(o) || used.count(o)) { bad = true; continue; }
+            used.insert(o);
+            const auto rc = dec[o];
+            int dre[OZ_NSLICE], dim[OZ_NSLICE];
+            oz_digits(psi[gi].real(), exm, dre);
+            oz_digits(psi[gi].imag(), exm, dim);
+            for (int s = 0; s < OZ_NSLICE; ++s) {
+              // the packed bf16 pair decodes to the digits
+              const uint32_t w = oz_bf16(dre[s]) | (oz_bf16(dim[s]) << 16);
+              uint32_t lo = (w & 0xFFFF) << 16, hi = w & 0xFFFF0000u;
+              float flo, fhi;
+              memcpy(&flo, &lo, 4);
+              memcpy(&fhi, &hi, 4);
+              if (flo != (float)dre[s] || fhi != (float)dim[s] || std::abs(dre[s]) > 128 || std::abs(dim[s]) > 128)
+                exact_fails++;
+              Ad[s][rc.first][2 * rc.second] = dre[s];
+              Ad[s][rc.first][2 * rc.second + 1] = dim[s];
+            }
+          }
+          if (t == 0)
+            for (int w = 0; w < OZ_THREADS / 32; ++w) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = geo->aoff_lo[32 * w + l] + geo->aoff_hi[r];
+              if (wavefronts(off, 4) > (t5 >= 2 ? 1 : t5 == 1 ? 2 : 4)) bank_fails++;
+            }
+        }
+        std::vector<cd> stage(OZ_TILE, cd(1e300, 0));
+        std::vector<double> bstage(OZ_TILE, 0.0);
+        for (int row = 0; row < 128; ++row)
+          for (int c = 0; c < 32; ++c) {
+            double vals[2];
+            for (int part = 0; part < 2; ++part) {
+              const int nn = 2 * c + part;
+              float acc[OZ_NLEVEL];
+              for (int l = 0; l < OZ_NLEVEL; ++l) {
+                int64_t sum = 0;
+                for (int i = std::max(0, l - (OZ_NSLICE - 1)); i <= std::min(l, OZ_NSLICE - 1); ++i)
+                  for (int k = 0; k < 64; ++k) sum += (int64_t)Ad[i][row][k] * Bd[l - i][nn][k];
+                if (std::llabs(sum) >= (1ll << 24)) exact_fails++;
+                acc[l] = (float)sum;
+              }
+              vals[part] = oz_combine(acc, exm + G->fexp[c] - 2098);
+            }
+            const uint32_t si = (uint32_t)row ^ geo->scol[c];
+            if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
+            stage[si] = cd(vals[0], vals[1]);
+            bstage[si] = std::ldexp(1.0, (exm - 1022) + (G->fexp[c] - 1022) - 41);
+          }
+        if (t == 0)
+          for (int w = 0; w < 4; ++w)
+            for (int c = 0; c < 32; ++c) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = 16 * ((uint32_t)(32 * w + l) ^ geo->scol[c]);
+              if (wavefronts(off, 16) > 4) bank_fails++;
+            }
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          for (int tid = 0; tid < OZ_THREADS; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            if (gi < 0 || gi >= N) { bad = true; continue; }
+            const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
+            if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
+            wrote[gi]++;
+            out[gi] = stage[si];
+            bound[gi] = bstage[si];
+          }
+          if (t == 0)
+            for (int w = 0; w < OZ_THREADS / 32; ++w) {
+              uint32_t off[32];
+              for (int l = 0; l < 32; ++l) off[l] = 16 * ((uint32_t)geo->sread_lo[32 * w + l] ^ geo->sread_hi[r]);
+              if (wavefronts(off, 16) > 4) bank_fails++;
+            }
+        }
+      }
+      double err = 0, nrm = 0;
+      int over = 0;
+      for (i64 i = 0; i < N; ++i) {
+        if (seen[i] != 1 || wrote[i] != 1) bad = true;
+        const double e = std::max(std::abs(out[i].real() - ref[i].real()), std::abs(out[i].imag() - ref[i].imag()));
+        if (e > bound[i]) over++;
+        err = std::max(err, std::abs(out[i] - ref[i]));
+        nrm = std::max(nrm, std::abs(ref[i]));
+      }
+      ++cases;
+      if (!wide) worst = std::max(worst, err / nrm);
+      if (bad || over || (!wide && err > 1e-13 * nrm)) {
+        ++fails;
+        printf("FAIL n=%d block bits %d,%d,%d,%d,%d rel err=%g bad=%d\n", n, tb[0], tb[1], tb[2], tb[3], tb[4],
+               err / nrm, (int)bad);
+        printf("  outputs over the bound: %d\n", over);
+      }
+      delete geo;
+      delete G;
+    }
+  }
+  printf("cases %d worst relative error (Gaussian states) %.3g\n", cases, worst);
+  printf("index failures %d exactness failures %d bank-pattern failures %d\n", fails, exact_fails, bank_fails);
+  return (fails || exact_fails || bank_fails) ? 1 : 0;
+}

@@ -1,8 +1,13 @@
-"""Tensor-core fused 5-qubit blocks (tcgen05, 3xTF32) against the FP64 oracle.
+"""Tensor-core fused 5-qubit blocks (tcgen05) against the FP64 oracle.
 
-Tolerance: 3xTF32 with FP32 accumulation reproduces FP32 arithmetic, so the
-complex64 result of one block matches the FP64 product to 2e-6 max-abs on a
-normalised state (and the kernel's own timeout flag stays clear)."""
+Tolerances: complex64 (3xTF32, FP32 accumulation) reproduces FP32 arithmetic,
+so one block matches the FP64 product to 2e-6 max-abs on a normalised state.
+complex128 (Ozaki scheme on BF16: 47-bit fixed point per tile and gate row,
+exact level accumulators) is bounded by 2^(E + F - 41) per output, with 2^E
+<= 2 x the largest |amplitude| and 2^F <= 2 x the largest |matrix entry|;
+the tests check that bound and 1e-13 absolute on normalised states, and
+1e-12 (the complex128 bar) on deep fused circuits.  The kernels' timeout
+flag must stay clear."""
 
 import ctypes as C
 
@@ -20,16 +25,16 @@ def _unitary(seed):
     return unitary_group.rvs(32, random_state=seed)
 
 
-def _apply_tc(psi, qubits, u):
+def _apply_tc(psi, qubits, u, dtype=np.complex64):
     from qibo_gb300 import _lib
     from qibo_gb300._lib import check
     from qibo_gb300.device import DeviceState, Runtime
 
     rt = Runtime.get()
     n = int(len(psi)).bit_length() - 1
-    st = DeviceState.from_numpy(psi.astype(np.complex64))
+    st = DeviceState.from_numpy(psi.astype(dtype))
     m = np.ascontiguousarray(u, dtype=np.complex128).view(np.float64).ravel()
-    check(rt.lib.qgb_apply_fused5_tc(st.ptr, n, _lib.int_array(qubits), m.ctypes.data_as(_lib.dp), rt.stream))
+    check(rt.lib.qgb_apply_fused5_tc(st.ptr, n, st.code, _lib.int_array(qubits), m.ctypes.data_as(_lib.dp), rt.stream))
     out = np.asarray(st)
     flag = C.c_int(-1)
     check(rt.lib.qgb_tc_status(C.byref(flag)))
@@ -66,3 +71,73 @@ def test_fused5_tc_block_of_a_brickwork():
     got = _apply_tc(psi, g.qubits, g.matrix())
     want = ref.apply_gate(psi, g.matrix(), list(g.qubits), n)
     assert np.max(np.abs(got - want)) < 2e-6
+
+
+def _rand_state(n, seed):
+    rng = np.random.default_rng(seed)
+    psi = rng.normal(size=2**n) + 1j * rng.normal(size=2**n)
+    return psi / np.linalg.norm(psi)
+
+
+def _oz_bound(psi, u):
+    return 4 * np.max(np.abs(psi)) * np.max(np.abs(u)) * 2.0**-41
+
+
+@pytest.mark.parametrize("n,qubits", [(12, (11, 3, 7, 0, 5)), (12, (0, 1, 2, 3, 4)), (13, (12, 11, 10, 9, 8)),
+                                      (16, (1, 15, 8, 4, 12)), (16, (2, 0, 14, 3, 9)), (17, (16, 13, 0, 7, 12))])
+def test_fused5_oz_complex128_matches_oracle(n, qubits):
+    psi = _rand_state(n, 100 + n)
+    u = _unitary(200 + n)
+    got = _apply_tc(psi, qubits, u, np.complex128)
+    want = ref.apply_gate(psi, u, list(qubits), n)
+    err = np.max(np.abs(got - want))
+    assert err < _oz_bound(psi, u) and err < 1e-13, err
+
+
+def test_fused5_oz_complex128_wide_range_and_zeros():
+    """Amplitudes over 2^-60..1 in one state, plus all-zero tiles."""
+    n = 14
+    rng = np.random.default_rng(9)
+    psi = (rng.normal(size=2**n) + 1j * rng.normal(size=2**n)) * 2.0 ** -rng.integers(0, 60, size=2**n)
+    psi[: 2**12] = 0  # whole tiles of zeros
+    u = _unitary(31)
+    got = _apply_tc(psi, (13, 2, 6, 9, 0), u, np.complex128)
+    want = ref.apply_gate(psi, u, [13, 2, 6, 9, 0], n)
+    assert np.max(np.abs(got - want)) < _oz_bound(psi, u)
+
+
+def test_fused5_oz_deep_fused_circuit():
+    """A depth-30 brickwork + QFT, fused into 5-qubit blocks, in complex128
+    through the blocked engine (tensor-core blocks + passes) against the FP64
+    oracle at the complex128 bar."""
+    from qibo_gb300 import Circuit, gates
+    from qibo_gb300.backend import GB300Backend
+
+    n = 16
+    ops = ref.brickwork_ops(n, 30, 5) + ref.qft_ops(n)
+    c = Circuit(n)
+    for nm, q, p in ops:
+        c.add(getattr(gates, nm)(*q, *p))
+    fused = c.fuse(5)
+    assert sum(1 for g in fused.queue if len(g.qubits) == 5) >= 20
+    psi = _rand_state(n, 77)
+    b = GB300Backend("complex128")
+    b.blocked = True
+    got = np.asarray(b.execute_circuit(fused, psi.copy()).state())
+    want = ref.execute(ops, n, psi)
+    assert np.max(np.abs(got - want)) < 1e-12
+    flag = C.c_int(-1)
+    check_status = b.rt.lib.qgb_tc_status(C.byref(flag))
+    assert check_status == 0 and flag.value == 0
+
+
+def test_fused5_oz_needs_twelve_qubits():
+    from qibo_gb300 import _lib
+    from qibo_gb300.device import DeviceState, Runtime
+
+    rt = Runtime.get()
+    st = DeviceState.from_numpy(_rand_state(11, 1))
+    m = np.ascontiguousarray(_unitary(3), dtype=np.complex128).view(np.float64).ravel()
+    with pytest.raises(NotImplementedError):
+        _lib.check(rt.lib.qgb_apply_fused5_tc(st.ptr, 11, st.code, _lib.int_array((0, 1, 2, 3, 4)),
+                                              m.ctypes.data_as(_lib.dp), rt.stream))

@@ -1,15 +1,16 @@
-"""CPU check of the tensor-core block kernel's index tables.
+"""CPU checks of the tensor-core block kernels' host logic.
 
-Compiles ``tests/native/tc_geometry_check.cu`` (which includes
-``qgb_tc.cu``) with nvcc and runs it on the host: it replays the kernel's
-loads, operand layout, permuted block product, staging and stores with the
-tables ``make_geom`` builds and compares against the block applied
-directly, and bounds the shared-memory wavefronts of every access pattern.
-No kernel is launched; nvcc cross-compiles here.
+Compiles ``tests/native/tc_geometry_check.cu`` (complex64, includes
+``qgb_tc.cu``) and ``tests/native/oz_check.cu`` (complex128 Ozaki scheme,
+includes ``qgb_tc128.cu``) with nvcc and runs them on the host: they replay
+each kernel's loads, operand layouts, products, staging and stores with the
+tables the launchers build (and, for complex128, the same digit / combine
+functions the kernel calls), compare against the block applied directly in
+FP64, and bound the shared-memory wavefronts of every access pattern.  No
+kernel is launched; nvcc cross-compiles here.
 """
 
 import os
-import shutil
 import subprocess
 
 import pytest
@@ -17,7 +18,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_tc_geometry_tables(tmp_path):
+def _build_and_run(tmp_path, name):
     from qibo_gb300 import _build
 
     try:
@@ -26,15 +27,25 @@ def test_tc_geometry_tables(tmp_path):
         pytest.skip("nvcc not available")
     if not os.path.exists(_build.LIB):
         _build.build()
-    exe = str(tmp_path / "tc_geometry_check")
+    exe = str(tmp_path / name)
     libdir = os.path.dirname(_build.LIB)
     libname = os.path.basename(_build.LIB)[3:-3]  # libqgb300.so -> qgb300
     cmd = [nvcc, *_build.ARCH, "-O2", "-std=c++17",
            "-I", os.path.join(ROOT, "qibo_gb300", "csrc"), "-I", os.path.join(ROOT, "include"),
-           os.path.join(ROOT, "tests", "native", "tc_geometry_check.cu"), "-o", exe,
+           os.path.join(ROOT, "tests", "native", name + ".cu"), "-o", exe,
            "-L", libdir, f"-l{libname}", "-Xlinker", f"-rpath,{libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
-    assert "index failures 0 bank-pattern failures 0" in r.stdout
+    return r.stdout
+
+
+def test_tc_geometry_tables(tmp_path):
+    out = _build_and_run(tmp_path, "tc_geometry_check")
+    assert "index failures 0 bank-pattern failures 0" in out
+
+
+def test_oz_complex128_blocks(tmp_path):
+    out = _build_and_run(tmp_path, "oz_check")
+    assert "index failures 0 exactness failures 0 bank-pattern failures 0" in out
