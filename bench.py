@@ -251,9 +251,11 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
             ms.append(ev.stop_ms(rt.stream))
         return ms
 
-    # complex128 blocked reference state
+    # complex128 reference state: the unfused gate list in double-float passes
     check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
+    ev.start(rt.stream)
     eng.apply_many(state, descs, blocked=True)
+    ms_128b = ev.stop_ms(rt.stream)
     timed(descs, 2)
     ms_p = timed(descs, 1)[0]
     norm_p = b64.engine_gb.renormalize(st64)  # FP64 renormalisation of the complex64 result
@@ -285,6 +287,16 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     eng.apply_many(state, descs, blocked=False)
     ms_g = ev.stop_ms(rt.stream)
     del st64
+    # the fused complex128 result (tensor-core blocks) against that IEEE FP64
+    # per-gate result: 1 - |<psi_per_gate|psi_fused>|^2 in FP64
+    st2 = DeviceState(n, "complex128")
+    check(lib.qgb_state_zero(st2.ptr, n, st2.code, rt.stream))
+    eng.apply_many(st2, fdescs, blocked=True)
+    check(lib.qgb_inner(state.ptr, st2.ptr, n, state.code, out.ptr, rt.scratch(lib.qgb_inner_scratch_bytes()),
+                        rt.stream))
+    re2, im2 = out.to_numpy()
+    inf_128 = 1.0 - (re2 * re2 + im2 * im2)
+    del st2
     g64, _ = algorithmic_bytes(n, ndense, ncz, 8)
     p50 = statistics.median(ms_f)
     p99 = ms_f[min(len(ms_f) - 1, int(np.ceil(0.99 * len(ms_f))) - 1)]
@@ -295,7 +307,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
                          "norm_before_renormalisation": norm_f, "tc_wait_timeouts": tc_timeout.value,
                          "k_fused5_tc_gbs": tc_gbs, "k_fused5_tc_bytes_per_launch": 2 * 2**n * 8,
                          "p99_note": "p99 of 8 runs is the slowest run"},
-            "c128_per_gate_ms": ms_g,
+            "c128_per_gate_ms": ms_g, "c128_unfused_passes_ms": ms_128b,
+            "c128_fused_infidelity_vs_per_gate_fp64": inf_128,
             "fused_tc_speedup_vs_c128_per_gate": ms_g / p50}
 
 
@@ -322,15 +335,28 @@ def run_brickwork(args):
     gates = brickwork_gates(n, DEPTH, SEED)
     circ = Circuit(n)
     circ.add(gates)
-    mode = args.mode if args.mode != "auto" else "blocked"
+    mode = args.mode if args.mode != "auto" else ("fused" if n >= 12 else "blocked")
+    t0 = time.perf_counter()
     run_circ = circ.fuse(5) if mode == "fused" else circ
+    fuse_s = time.perf_counter() - t0
     descs = [describe_gate(g, backend) for g in run_circ.queue]
+    udescs = descs if run_circ is circ else [describe_gate(g, backend) for g in circ.queue]
     backend.blocked = mode in ("blocked", "fused")
     ndense = sum(1 for g in gates if type(g).__name__ == "U3")
     ncz = len(gates) - ndense
     gbytes, mbytes = algorithmic_bytes(n, ndense, ncz, S)
     code = 1 if dtype == "complex128" else 0
-    npasses = eng.count_passes(n, code, descs) if backend.blocked else len(descs)
+    # state passes the engine makes: tensor-core blocks (uncontrolled 5-qubit
+    # dense ops) one each, the ops between them planned into shared-memory passes
+    is_tc = [mode == "fused" and len(d[0]) == 5 and not d[1] for d in descs]
+    n_tc, npasses, seg = sum(is_tc), 0, []
+    for d, tc in zip(descs + [None], is_tc + [True]):
+        if tc:
+            npasses += eng.count_passes(n, code, seg) if (seg and backend.blocked) else len(seg)
+            seg = []
+        else:
+            seg.append(d)
+    npasses += n_tc
     pass_bytes = (npasses * 2 * 2**n * S) if backend.blocked else gbytes
     state = DeviceState(n, dtype)
     allq = list(range(n))
@@ -375,17 +401,44 @@ def run_brickwork(args):
     ev.start(rt.stream)
     eng.apply_many(state, descs, blocked=backend.blocked)
     gate_ms = ev.stop_ms(rt.stream)
-    k_ms = gate_ms / max(1, npasses)
-    k_bytes = pass_bytes / max(1, npasses)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
-    roof = {"bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "traffic": 2.09e9 * (2 ** (n - 26)) if n >= 26 else None,
-            "traffic_note": "dram bytes per k_pass launch from ncu at n=26 (1.075 GB read + 1.014 GB write), "
-                            "scaled by 2^(n-26); equals the algorithmic bytes",
-            "kernel": "k_pass (shared-memory multi-gate pass)" if backend.blocked else "per-gate kernels",
-            "per_launch_bytes": k_bytes, "launches": npasses,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
+    peak_source = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+    if n_tc:
+        # dominant kernel: the tensor-core block kernel, 10 launches of the
+        # circuit's first block, CUDA events on the launch stream
+        from qibo_gb300 import _lib
+
+        blk = next(d for d, tc in zip(descs, is_tc) if tc)
+        qs = _lib.int_array(blk[0])
+        mat = np.ascontiguousarray(np.asarray(blk[2], dtype=np.complex128)).view(np.float64).ravel()
+        mp = mat.ctypes.data_as(_lib.dp)
+        check(lib.qgb_apply_fused5_tc(state.ptr, n, state.code, qs, mp, rt.stream))
+        ev.start(rt.stream)
+        for _ in range(10):
+            check(lib.qgb_apply_fused5_tc(state.ptr, n, state.code, qs, mp, rt.stream))
+        k_ms = ev.stop_ms(rt.stream) / 10
+        k_bytes = 2 * 2**n * S
+        # dram bytes of one launch at n=28 from ncu, scaled by 2^(n-28)
+        traffic28 = (4.295e9 + 4.233e9) if S == 16 else (2.148e9 + 2.086e9)
+        kname = "k_fused5_oz (complex128 Ozaki scheme on BF16 tensor cores)" if S == 16 else \
+            "k_fused5_tc (complex64 3xTF32 tensor cores)"
+        roof = {"bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak, "traffic": traffic28 * 2 ** (n - 28),
+                "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one launch from ncu at n=28, "
+                                "scaled by 2^(n-28); equals the algorithmic bytes",
+                "kernel": kname, "per_launch_bytes": k_bytes, "launches": n_tc, "ms_per_launch": k_ms,
+                "share_of_gate_time": n_tc * k_ms / gate_ms, "peak_source": peak_source}
+    else:
+        k_ms = gate_ms / max(1, npasses)
+        k_bytes = pass_bytes / max(1, npasses)
+        roof = {"bound": "hbm", "achieved": k_bytes / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": k_bytes / (k_ms * 1e-3) / 1e9 / peak,
+                "traffic": 2.09e9 * (2 ** (n - 26)) if n >= 26 else None,
+                "traffic_note": "dram bytes per k_pass launch from ncu at n=26 (1.075 GB read + 1.014 GB write), "
+                                "scaled by 2^(n-26); equals the algorithmic bytes",
+                "kernel": "k_pass (shared-memory multi-gate pass)" if backend.blocked else "per-gate kernels",
+                "per_launch_bytes": k_bytes, "launches": npasses, "peak_source": peak_source}
 
     # end to end through the public API: host circuit in, 1e6 samples out
     e2e_times = []
@@ -403,10 +456,14 @@ def run_brickwork(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128" if dtype == "complex128" else "c64", "data": "synthetic",
             "config": {"workload": f"random U3+CZ brickwork n={n} depth {DEPTH} seed {SEED} + {NSHOTS} shots",
-                       "mode": mode, "gates": len(gates), "state_passes": npasses,
-                       "arithmetic": ("double-float (FP32 pipe) in passes, IEEE FP64 reductions"
-                                      if dtype == "complex128" and backend.blocked and not backend.strict_fp64
-                                      else "native"),
+                       "mode": mode, "gates": len(gates), "state_passes": npasses, "tensor_core_blocks": n_tc,
+                       "fusion": ("qibo Circuit.fuse(max_qubits=5), once before timing "
+                                  f"({fuse_s:.2f} s, {len(descs)} blocks)") if mode == "fused" else "none",
+                       "arithmetic": (("5-qubit blocks: Ozaki scheme on BF16 tensor cores (47-bit fixed point, "
+                                       "exact level sums, IEEE doubles out); " if n_tc and S == 16 else "")
+                                      + ("double-float (FP32 pipe) in passes, IEEE FP64 reductions"
+                                         if dtype == "complex128" and backend.blocked and not backend.strict_fp64
+                                         else "native")),
                        "bytes": "effective: per-gate algorithmic bytes of the unfused circuit + probabilities + CDF",
                        "l2": "state 2^n*S >> L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single"},
@@ -416,8 +473,8 @@ def run_brickwork(args):
             "e2e": {"value": total_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": coef_bytes,
                     "d2h_bytes_per_step": NSHOTS * 8, "seconds": e2e_s}}
 
-    if dtype == "complex128" and rank == 0 and not args.quick and mode != "fused":
-        line["complex64"] = complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz)
+    if dtype == "complex128" and rank == 0 and not args.quick:
+        line["complex64"] = complex64_legs(args, n, circ, udescs, state, backend, ev, ndense, ncz)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0 and world == 1 and args.serving_requests > 0:
@@ -491,7 +548,9 @@ def run_tc5(args):
     a state of ``--nqubits`` qubits (default 30; 8.6 GB in complex64, 17.2 GB
     in complex128, inputs >> L2), one launch per step, for three placements
     of the block qubits (lowest index bits, highest, spread), in complex64
-    (k_fused5_tc, 3xTF32) and complex128 (k_fused5_oz, Ozaki scheme on BF16).
+    (k_fused5_tc, 3xTF32) and complex128 (k_fused5_oz, Ozaki scheme on BF16;
+    single launches on IEEE doubles, and a chain of 10 blocks in the
+    fixed-point format through qgb_apply_circuit), on a dense state.
     Algorithmic bytes per launch: 2 * 2^n * S."""
     from qibo_gb300 import _lib
     from qibo_gb300._lib import check
@@ -513,6 +572,11 @@ def run_tc5(args):
                                      ("complex128", "k_fused5_oz", 16, 26 * 2 * 64 * 64)):
         st = DeviceState(n, dtype)
         check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+        # a dense state (the kernels' cost depends on the data: zero tiles are
+        # cheaper): the random unitary on qubits 5k..5k+4 for every k
+        for k in range(n // 5):
+            check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, _lib.int_array(range(5 * k, 5 * k + 5)), mp,
+                                          rt.stream))
         nbytes = 2 * 2**n * S
         res = {"kernel": kernel, "bytes_per_launch": nbytes}
         for name, qs in (("high_bits", [0, 1, 2, 3, 4]), ("low_bits", [n - 1, n - 2, n - 3, n - 4, n - 5]),
@@ -527,6 +591,20 @@ def run_tc5(args):
             gbs = nbytes / (ms * 1e-3) / 1e9
             res[name] = {"qubits": qs, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
                          "tensor_tflops": flops * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
+        if dtype == "complex128":
+            # a chain of 10 unitary blocks through qgb_apply_circuit: the state
+            # is converted once to the fixed-point format (norm pass + 2
+            # conversion passes, amortised below) and the blocks run on it
+            descs = [([1, n // 3, n // 2, n - 3, n - 1], [], u)] * 10
+            b128 = GB300Backend("complex128")
+            b128.engine_gb.apply_many(st, descs, blocked=True)
+            ev.start(rt.stream)
+            b128.engine_gb.apply_many(st, descs, blocked=True)
+            ms = ev.stop_ms(rt.stream) / 10
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            res["fixed_point_chain_of_10"] = {"kernel": "k_fused5_oz<fixed-point>", "ms_per_block": ms, "GB/s": gbs,
+                                              "frac_of_measured_hbm": gbs / peak,
+                                              "note": "includes the norm and the two conversion passes"}
         out[dtype] = res
         del st
     flag = C.c_int(0)

@@ -233,8 +233,6 @@ int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vect
 
 }  // namespace
 
-int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc.cu
-int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc128.cu
 
 namespace {
 bool is_tc_block(const GateOp& g) { return g.kind == GK_DENSE && g.tbits.size() == 5 && g.cbits.empty(); }
@@ -274,22 +272,47 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
   }
   const bool tc_ok = use_tc && (dtype == QGB_C64 || (dtype == QGB_C128 && nqubits >= 12 && !strict_fp64));
   if (!tc_ok) return run_segment(state, nqubits, dtype, g, strict_fp64, s);
+  // consecutive tensor-core blocks; a complex128 run of two or more unitary
+  // blocks runs as one fixed-point chain
+  std::vector<const GateOp*> run;
+  auto flush_run = [&]() -> int {
+    if (run.empty()) return QGB_OK;
+    int st = QGB_OK;
+    bool chain = dtype == QGB_C128 && run.size() >= 2;
+    for (const GateOp* b : run) chain = chain && qgb_oz_unitary(*b);
+    if (chain) {
+      st = qgb_run_oz_chain(state, nqubits, run, s);
+    } else {
+      for (const GateOp* b : run) {
+        st = dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, *b, s, false)
+                               : qgb_launch_fused5_tc(state, nqubits, *b, s);
+        if (st) break;
+      }
+    }
+    run.clear();
+    return st;
+  };
   std::vector<GateOp> seg;
   for (int i = 0; i <= nops; ++i) {
     const bool tc = i < nops && is_tc_block(g[i]);
-    if (i == nops || tc) {
+    if (tc) {
       if (!seg.empty()) {
         int st = run_segment(state, nqubits, dtype, seg, strict_fp64, s);
         if (st) return st;
         seg.clear();
       }
-      if (tc) {
-        int st = dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, g[i], s)
-                                   : qgb_launch_fused5_tc(state, nqubits, g[i], s);
-        if (st) return st;
-      }
+      run.push_back(&g[i]);
     } else {
-      seg.push_back(g[i]);
+      int st = flush_run();
+      if (st) return st;
+      if (i == nops) {
+        if (!seg.empty()) {
+          st = run_segment(state, nqubits, dtype, seg, strict_fp64, s);
+          if (st) return st;
+        }
+      } else {
+        seg.push_back(g[i]);
+      }
     }
   }
   return QGB_OK;

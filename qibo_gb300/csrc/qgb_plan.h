@@ -30,3 +30,11 @@ struct GateOp {
 // Returns a QGB status; on success fills ``op``.
 int qgb_classify(int nqubits, const int* qubits, int k, const int* controls, int ncontrols,
                  const double* matrix, GateOp* op, const char* fn);
+
+// Tensor-core block kernels (qgb_tc.cu, qgb_tc128.cu): uncontrolled 5-qubit
+// dense blocks.  complex64 3xTF32; complex128 Ozaki scheme (n >= 12), on
+// IEEE doubles or, inside a chain, on the fixed-point format.
+int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix);
+bool qgb_oz_unitary(const GateOp& g);
+int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);

@@ -367,8 +367,6 @@ void set_tc_smem_attr() {
 }
 }  // namespace
 
-int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s);  // qgb_tc128.cu
-
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   if (g.tbits.size() != 5 || !g.cbits.empty() || n < 5) {
     qgb_set_error("qgb_apply_fused5_tc: needs an uncontrolled 5-qubit dense block");
@@ -425,7 +423,7 @@ int qgb_apply_fused5_tc(void* state, int nqubits, int dtype, const int* qubits, 
   for (int j = 0; j < 5; ++j) g.tbits.push_back(nqubits - 1 - qubits[j]);
   g.coef.resize(1024);
   for (int i = 0; i < 1024; ++i) g.coef[i] = zd(matrix[2 * i], matrix[2 * i + 1]);
-  return dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, g, (cudaStream_t)stream)
+  return dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, g, (cudaStream_t)stream, false)
                            : qgb_launch_fused5_tc(state, nqubits, g, (cudaStream_t)stream);
 }
 

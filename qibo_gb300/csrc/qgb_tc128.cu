@@ -33,9 +33,11 @@
 // level 6 is its own instruction so that it starts the accumulation), 37
 // per tile.
 //
-// A CTA (256 threads, one per SM: 223 KB of shared memory, 384 TMEM columns)
-// owns 4096-amplitude tiles with the index geometry of qgb_tc.cu; the next
-// tile is prefetched into registers while the MMAs run.  The wait on the
+// A CTA (512 threads, one per SM: 223 KB of shared memory, 448 TMEM columns)
+// owns 4096-amplitude tiles with the index geometry of qgb_tc.cu (thread t
+// moves amplitudes t + 512 r, r < 8); the next tile is prefetched into
+// registers while the MMAs run.  The digit split and the combination are
+// integer work on the ALU pipe; 16 warps keep it issuing.  The wait on the
 // mbarrier is bounded: on timeout the kernel records an error flag, waits
 // once more (bounded) for the in-flight MMAs, frees its tensor memory and
 // returns.
@@ -47,8 +49,8 @@
 #include "qgb_plan.h"
 #include "qgb_tcgen05.cuh"
 
-#define OZ_THREADS 256
-#define OZ_STEPS 16    // amplitudes per thread per tile
+#define OZ_THREADS 512
+#define OZ_STEPS 8     // amplitudes per thread per tile
 #define OZ_TILE 4096   // amplitudes per tile
 #define OZ_NSLICE 6    // digits per value
 #define OZ_NLEVEL 7    // digit-product levels kept (i + j <= 6)
@@ -71,9 +73,10 @@ static_assert(OZ_OFF_B % 16 == 0 && OZ_OFF_STAGE % 16 == 0, "operand regions 16-
 static_assert(OZ_SMEM <= 227 * 1024, "one CTA per SM");
 static_assert(OZ_THREADS * OZ_STEPS == OZ_TILE, "one amplitude per thread and step");
 
-// Tile geometry (same tile / thread mapping as the complex64 kernel): tile
-// index j = t + 256 r has global offset base + (t & 127) + (t >> 7) g7 +
-// ghi[r]; its (re, im) bf16 pair sits at byte aoff_lo[t] + aoff_hi[r] of
+// Tile geometry (the tile of the complex64 kernel): tile index
+// j = t + 512 r has global offset base + (t & 127) + t7 g7 + t8 g8 + ghi[r]
+// (t7, t8 bits 7 and 8 of t); its (re, im) bf16 pair sits at byte
+// aoff_lo[t] + aoff_hi[r] of
 // every A slice; staging slot of (row, column c) is
 //   (c << 7 | row) ^ ((c << g3) & 7),   g3 = 3 - (block qubits on bits 0..2),
 // written as row ^ scol[c] and read as sread_lo[t] ^ sread_hi[r].
@@ -81,7 +84,7 @@ struct OzGeom {
   int nrest;
   int rest[32];
   uint32_t a_lbo;
-  i64 g7;
+  i64 g7, g8;
   i64 ghi[OZ_STEPS];
   uint32_t aoff_lo[OZ_THREADS];
   uint32_t aoff_hi[OZ_STEPS];
@@ -128,29 +131,71 @@ __host__ __device__ __forceinline__ uint32_t oz_fbits(float x) {
 #endif
 }
 
-// Balanced base-256 digits of x in 47-bit fixed point against exponent exm
-// (the biased exponent of the largest |value| sharing the scale):
-//   x ~= 2^(exm - 1069) * sum_{i<6} d[i] 256^(5-i),   |d[i]| <= 128,
-// rounding error <= 2^(exm - 1070); values below 2^-58 of the scale and
-// subnormals become 0.
-__host__ __device__ __forceinline__ void oz_digits(double x, int exm, int d[OZ_NSLICE]) {
+// 47-bit fixed-point value of x against exponent exm (the biased exponent
+// of the largest |value| sharing the scale): X = round(x 2^(1069 - exm)),
+// |X| <= 2^47, rounding error <= 2^(exm - 1070) in x; values below 2^-58 of
+// the scale and subnormals become 0.
+__host__ __device__ __forceinline__ int64_t oz_fix47(double x, int exm) {
   const uint64_t u = oz_dbits(x);
-  const int ex = (int)((u >> 52) & 0x7FF);
+  const uint32_t hi = (uint32_t)(u >> 32);
+  const int ex = (int)((hi >> 20) & 0x7FF);
   const int rs = 6 + exm - ex;
-  int64_t X = 0;
-  if (ex != 0 && rs < 60) {
-    const uint64_t M = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    X = (int64_t)((M + (1ull << (rs - 1))) >> rs);
-    if (u >> 63) X = -X;
-  }
-  // bottom-up: d = sign-extended low byte, X <- (X - d) / 256 (exact)
+  if (ex == 0 || rs >= 60) return 0;
+  const uint64_t M = ((uint64_t)((hi & 0xFFFFFu) | 0x100000u) << 32) | (uint32_t)u;
+  const int64_t X = (int64_t)(((M >> (rs - 1)) + 1) >> 1);  // round half up
+  return (int32_t)hi < 0 ? -X : X;
+}
+
+// exact float of an integer 0 <= c < 2^23, and of |c| < 2^22
+__host__ __device__ __forceinline__ float oz_u2f(uint32_t c) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(0x4B000000u | c) - 8388608.0f;
+#else
+  return (float)c;
+#endif
+}
+__host__ __device__ __forceinline__ float oz_i2f(int32_t c) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(0x4B400000 + c) - 12582912.0f;
+#else
+  return (float)c;
+#endif
+}
+
+// nearest integer, ties to even, of |v| < 2^22, as a float (IEEE addition:
+// neither compiler folds (v + C) - C without fast-math)
+__host__ __device__ __forceinline__ float oz_rintf(float v) { return (v + 12582912.0f) - 12582912.0f; }
+
+// Balanced base-256 digits of a 47-bit fixed-point value, as exact floats:
+//   X = sum_{i<6} d[i] 256^(5-i),   |d[i]| <= 128.
+// X splits into a signed top (bits 32..47) and two 16-bit chunks, each
+// converted exactly to FP32; every digit is then w - 256 rint(w / 256) on
+// the FMA pipe, carrying rint(.) upwards.
+__host__ __device__ __forceinline__ void oz_digits_f(int64_t X, float d[OZ_NSLICE]) {
+  const uint32_t lo = (uint32_t)X;
+  const int32_t hi = (int32_t)(X >> 32);
+  float w = oz_u2f(lo & 0xFFFFu);
+  float q = oz_rintf(w * 0.00390625f);
+  d[5] = w - 256.0f * q;
+  float t = oz_rintf(q * 0.00390625f);
+  d[4] = q - 256.0f * t;
+  w = oz_u2f(lo >> 16) + t;
+  q = oz_rintf(w * 0.00390625f);
+  d[3] = w - 256.0f * q;
+  t = oz_rintf(q * 0.00390625f);
+  d[2] = q - 256.0f * t;
+  w = oz_i2f(hi) + t;
+  q = oz_rintf(w * 0.00390625f);
+  d[1] = w - 256.0f * q;
+  d[0] = q;
+}
+
+// the same digits as integers (host checks and the B slices)
+__host__ __device__ __forceinline__ void oz_digits(double x, int exm, int d[OZ_NSLICE]) {
+  float f[OZ_NSLICE];
+  oz_digits_f(oz_fix47(x, exm), f);
 #pragma unroll
-  for (int i = OZ_NSLICE - 1; i >= 1; --i) {
-    const int di = (int)(int8_t)(uint8_t)(X & 0xFF);
-    d[i] = di;
-    X = (X - di) >> 8;
-  }
-  d[0] = (int)X;
+  for (int i = 0; i < OZ_NSLICE; ++i) d[i] = (int)f[i];
 }
 
 // bf16 bit pattern of an integer |d| <= 256 (exact)
@@ -163,13 +208,13 @@ __host__ __device__ __forceinline__ uint32_t oz_bf16(int d) {
   return oz_fbits(f) >> 16;
 }
 
-// integer value of an integer-valued float: exact for |v| <= 2^22; for
-// 2^22 < |v| < 2^24 rounded to a multiple of 4 (wide = true)
-__host__ __device__ __forceinline__ int oz_f2i(float v, bool wide) {
+// (re, im) digit pair as packed bf16x2 (re in the low half); the digits are
+// integers |d| <= 128, exact in bf16
+__host__ __device__ __forceinline__ uint32_t oz_pack(float dre, float dim) {
 #ifdef __CUDA_ARCH__
-  return wide ? (__float_as_int(v + 50331648.0f) - 0x4C400000) * 4 : __float_as_int(v + 12582912.0f) - 0x4B400000;
+  return __byte_perm(__float_as_uint(dre), __float_as_uint(dim), 0x7632);
 #else
-  return wide ? 4 * (int)std::nearbyint((double)v / 4.0) : (int)v;  // ties to even, as the FADD
+  return (oz_fbits(dre) >> 16) | (oz_fbits(dim) & 0xFFFF0000u);
 #endif
 }
 
@@ -181,29 +226,78 @@ __host__ __device__ __forceinline__ int oz_clz64(uint64_t a) {
 #endif
 }
 
-// (sum_{l<=5} acc[l] 256^(5-l) + round(acc[6] / 256)) * 2^sc as an IEEE
-// double (one rounding, to nearest even); acc[l] are the level accumulators
-// (integers in floats)
-__host__ __device__ __forceinline__ double oz_combine(const float acc[OZ_NLEVEL], int sc) {
-  int64_t T = ((int64_t)oz_f2i(acc[6], true) + 128) >> 8;
-#pragma unroll
-  for (int l = 0; l < OZ_NSLICE; ++l) T += (int64_t)oz_f2i(acc[l], l >= 4) * ((int64_t)1 << (8 * (OZ_NSLICE - 1 - l)));
+// T * 2^sc as an IEEE double (one rounding, to nearest even; 0 below the
+// normal range)
+__host__ __device__ __forceinline__ double oz_i64_to_double(int64_t T, int sc) {
   if (T == 0) return 0.0;
-  const uint64_t s = T < 0 ? (1ull << 63) : 0;
-  const uint64_t a = T < 0 ? (uint64_t)(-T) : (uint64_t)T;
-  const int p = 63 - oz_clz64(a);  // top bit
-  const int be = p + sc + 1023;    // biased exponent of the result
-  if (be <= 0) return oz_bitsd(s);  // below the normal range: 0
-  uint64_t mant;
-  if (p > 52) {
-    const int r = p - 52;
-    mant = a >> r;
-    const uint64_t rem = a & ((1ull << r) - 1), half = 1ull << (r - 1);
-    if (rem > half || (rem == half && (mant & 1))) mant += 1;
-  } else {
-    mant = a << (52 - p);
-  }
+  const uint64_t s = (uint64_t)T & (1ull << 63);
+  uint64_t a = T < 0 ? (uint64_t)(-T) : (uint64_t)T;
+  const int lz = oz_clz64(a);
+  a <<= lz;  // top bit at 63
+  uint64_t mant = a >> 11;
+  const uint32_t rb = (uint32_t)a & 0x7FFu;
+  mant += (rb > 0x400u || (rb == 0x400u && (mant & 1))) ? 1 : 0;
+  const int be = 63 - lz + sc + 1023;  // biased exponent of the result
+  if (be <= 0) return oz_bitsd(s);
   return oz_bitsd(s | (((uint64_t)(be - 1) << 52) + mant));
+}
+
+// The level accumulators (integers in floats; levels 0..3 are below 2^22 and
+// converted exactly, levels 4..6 only need their top bits) as
+//   T = sum_{l<=3} acc[l] 256^(5-l) + 4 round(acc[4]/4) 256 + 4 round(acc[5]/4)
+//       + round(acc[6]/256).
+// Each level is rounded by a magic-constant addition on the FMA pipe; the
+// integer then sits in the raw bits minus 0x4B400000, and that offset is
+// folded into one constant of the multiply-add chain.
+__host__ __device__ __forceinline__ int64_t oz_levels(const float acc[OZ_NLEVEL]) {
+  const int32_t K = 0x4B400000;
+  const float C = 12582912.0f;
+  const int32_t b0 = (int32_t)oz_fbits(acc[0] + C), b1 = (int32_t)oz_fbits(acc[1] + C);
+  const int32_t b2 = (int32_t)oz_fbits(acc[2] + C), b3 = (int32_t)oz_fbits(acc[3] + C);
+  const int32_t b4 = (int32_t)oz_fbits(acc[4] * 0.25f + C), b5 = (int32_t)oz_fbits(acc[5] * 0.25f + C);
+  const int32_t b6 = (int32_t)oz_fbits(acc[6] * 0.00390625f + C);
+  const int32_t H = (b0 - K) * 256 + (b1 - K);
+  const int64_t L = (int64_t)b2 * 16777216 + (int64_t)b3 * 65536 + (int64_t)b4 * 1024 + (int64_t)b5 * 4 +
+                    (int64_t)b6 - (int64_t)K * (16777216 + 65536 + 1024 + 4 + 1);
+  return L + (int64_t)H * ((int64_t)1 << 32);
+}
+
+// T * 2^sc as an IEEE double
+__host__ __device__ __forceinline__ double oz_combine(const float acc[OZ_NLEVEL], int sc) {
+  return oz_i64_to_double(oz_levels(acc), sc);
+}
+
+// round(T * 2^k) as a 64-bit integer (fixed-point output; |result| < 2^62)
+__host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NLEVEL], int k) {
+  const int64_t T = oz_levels(acc);
+  if (k >= 0) return T * ((int64_t)1 << k);
+  if (k <= -63) return 0;
+  return (T + ((int64_t)1 << (-k - 1))) >> (-k);
+}
+
+// Fixed-point state format between consecutive tensor-core blocks: a real
+// x is held as the integer X = round(x 2^(62 - e)), e a state-wide scale with
+// 2^e > 2 ||psi|| (so |X| < 2^61, and unitary blocks keep it there).
+__host__ __device__ __forceinline__ int64_t oz_to_fix(double x, int e) {
+  const uint64_t u = oz_dbits(x);
+  const uint32_t hi = (uint32_t)(u >> 32);
+  const int ex = (int)((hi >> 20) & 0x7FF);
+  if (ex == 0) return 0;
+  const uint64_t M = ((uint64_t)((hi & 0xFFFFFu) | 0x100000u) << 32) | (uint32_t)u;
+  const int sh = ex - 1013 - e;  // X = M 2^sh
+  int64_t X;
+  if (sh >= 0) X = (int64_t)(M << (sh < 8 ? sh : 8));  // sh <= 8 when |x| < 2^(e-1)
+  else if (sh <= -60) X = 0;
+  else X = (int64_t)(((M >> (-sh - 1)) + 1) >> 1);
+  return (int32_t)hi < 0 ? -X : X;
+}
+
+__host__ __device__ __forceinline__ double oz_from_fix(int64_t X, int e) { return oz_i64_to_double(X, e - 62); }
+
+// 47-bit value of a fixed-point X at tile shift sh (the tile's largest |X|
+// is below 2^(47 + sh)), rounding half up
+__host__ __device__ __forceinline__ int64_t oz_fix47_fix(int64_t X, int sh) {
+  return sh > 0 ? (X + ((int64_t)1 << (sh - 1))) >> sh : X;
 }
 
 // byte offset of element (row, k) of the stacked B slices (dense, K-major)
@@ -223,6 +317,9 @@ __device__ __forceinline__ void oz_mma(uint32_t d, uint64_t a, uint64_t b, uint3
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
+// FIX: the state holds fixed-point integers (oz_to_fix) instead of IEEE
+// doubles; the tile scale is then a shift and the output a rounding shift.
+template <bool FIX>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_fused5_oz(double2* __restrict__ psi, i64 ntiles, const __grid_constant__ OzGeom geo,
                 const __grid_constant__ OzGate G, int* __restrict__ err) {
@@ -230,7 +327,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ uint32_t red[OZ_THREADS / 32];
+  __shared__ uint32_t red[OZ_THREADS / 32], red_hi[OZ_THREADS / 32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t s_base = smem_u32(sm);
   const uint32_t mb = smem_u32(&mbar);
@@ -266,11 +363,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const uint32_t srd = geo.sread_lo[tid];
   const uint32_t a_lbo = geo.a_lbo;
   const int my_rest = lane < geo.nrest ? geo.rest[lane] : -1;
-  const i64 toff = (i64)(tid & 127) + ((tid >> 7) ? geo.g7 : 0);
+  const i64 toff = (i64)(tid & 127) + (((tid >> 7) & 1) ? geo.g7 : 0) + ((tid >> 8) ? geo.g8 : 0);
   double2* stage = (double2*)(sm + OZ_OFF_STAGE);
-  // epilogue: this warp's TMEM sub-partition (group rows) and column half
+  // epilogue: this warp's TMEM sub-partition (group rows) and column quarter
   const int erow = 32 * (warp & 3) + lane;
-  const int ehalf = warp >> 2;
+  const int equart = warp >> 2;
   const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
 
   double2 v[OZ_STEPS];
@@ -283,29 +380,57 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
   }
   for (; t < ntiles; t += gridDim.x) {
-    // tile scale: the largest biased exponent among the tile's 8192 values
-    uint32_t m = 0;
+    // tile scale: doubles -- the largest biased exponent among the tile's
+    // 8192 values; fixed point -- the top bit of the OR of their magnitudes
+    int exm = 0, sh = 0;
+    if (FIX) {
+      uint64_t o = 0;
 #pragma unroll
-    for (int r = 0; r < OZ_STEPS; ++r) {
-      m = max(m, (uint32_t)(oz_dbits(v[r].x) >> 32) & 0x7FF00000u);
-      m = max(m, (uint32_t)(oz_dbits(v[r].y) >> 32) & 0x7FF00000u);
+      for (int r = 0; r < OZ_STEPS; ++r) {
+        const int64_t a = (int64_t)oz_dbits(v[r].x), b = (int64_t)oz_dbits(v[r].y);
+        o |= (uint64_t)(a < 0 ? -a : a) | (uint64_t)(b < 0 ? -b : b);
+      }
+      const uint32_t olo = __reduce_or_sync(0xffffffffu, (uint32_t)o);
+      const uint32_t ohi = __reduce_or_sync(0xffffffffu, (uint32_t)(o >> 32));
+      if (lane == 0) {
+        red[warp] = olo;
+        red_hi[warp] = ohi;
+      }
+      __syncthreads();
+      uint64_t ot = 0;
+#pragma unroll
+      for (int w = 0; w < OZ_THREADS / 32; ++w) ot |= ((uint64_t)red_hi[w] << 32) | red[w];
+      const int p = ot ? 63 - oz_clz64(ot) : -1;
+      sh = p > 46 ? p - 46 : 0;
+    } else {
+      uint32_t m = 0;
+#pragma unroll
+      for (int r = 0; r < OZ_STEPS; ++r) {
+        m = max(m, (uint32_t)(oz_dbits(v[r].x) >> 32) & 0x7FF00000u);
+        m = max(m, (uint32_t)(oz_dbits(v[r].y) >> 32) & 0x7FF00000u);
+      }
+      m = __reduce_max_sync(0xffffffffu, m);
+      if (lane == 0) red[warp] = m;
+      __syncthreads();
+      uint32_t mx = red[0];
+#pragma unroll
+      for (int w = 1; w < OZ_THREADS / 32; ++w) mx = max(mx, red[w]);
+      exm = (int)(mx >> 20);
     }
-    m = __reduce_max_sync(0xffffffffu, m);
-    if (lane == 0) red[warp] = m;
-    __syncthreads();
-    uint32_t mx = red[0];
-#pragma unroll
-    for (int w = 1; w < OZ_THREADS / 32; ++w) mx = max(mx, red[w]);
-    const int exm = (int)(mx >> 20);
     // digits -> A slices (one (re, im) bf16 pair per slice and amplitude)
 #pragma unroll
     for (int r = 0; r < OZ_STEPS; ++r) {
-      int dre[OZ_NSLICE], dim[OZ_NSLICE];
-      oz_digits(v[r].x, exm, dre);
-      oz_digits(v[r].y, exm, dim);
+      float dre[OZ_NSLICE], dim[OZ_NSLICE];
+      if (FIX) {
+        oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].x), sh), dre);
+        oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].y), sh), dim);
+      } else {
+        oz_digits_f(oz_fix47(v[r].x, exm), dre);
+        oz_digits_f(oz_fix47(v[r].y, exm), dim);
+      }
       unsigned char* a = sm + OZ_OFF_A + aoff + geo.aoff_hi[r];
 #pragma unroll
-      for (int s = 0; s < OZ_NSLICE; ++s) *(uint32_t*)(a + s * OZ_A_SLICE) = oz_bf16(dre[s]) | (oz_bf16(dim[s]) << 16);
+      for (int s = 0; s < OZ_NSLICE; ++s) *(uint32_t*)(a + s * OZ_A_SLICE) = oz_pack(dre[s], dim[s]);
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -360,24 +485,30 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // epilogue: combine the six levels of 8 reals at a time into doubles
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    // epilogue: combine the seven levels of 8 reals (4 amplitudes) at a time
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
       float acc[OZ_NLEVEL][8];
 #pragma unroll
-      for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(trow + 64 * l + 32 * ehalf + 8 * q, acc[l]);
+      for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(trow + 64 * l + 16 * equart + 8 * h, acc[l]);
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
       for (int e = 0; e < 8; e += 2) {
-        const int c = 16 * ehalf + 4 * q + (e >> 1);  // output amplitude (permuted block index)
-        const int sc = exm + G.fexp[c] - 2098;
+        const int c = 8 * equart + 4 * h + (e >> 1);  // output amplitude (permuted block index)
         float are[OZ_NLEVEL], aim[OZ_NLEVEL];
 #pragma unroll
         for (int l = 0; l < OZ_NLEVEL; ++l) {
           are[l] = acc[l][e];
           aim[l] = acc[l][e + 1];
         }
-        stage[erow ^ geo.scol[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+        if (FIX) {
+          const int k = sh + G.fexp[c] - 1029;
+          stage[erow ^ geo.scol[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
+                                                   oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
+        } else {
+          const int sc = exm + G.fexp[c] - 2098;
+          stage[erow ^ geo.scol[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+        }
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -453,15 +584,16 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
   for (int v = 0; v < OZ_THREADS; ++v) {
     i64 dep;
     uint32_t row, col;
-    split(v, 0, 8, &dep, &row, &col);
+    split(v, 0, 9, &dep, &row, &col);
     geo->aoff_lo[v] = aoff(row, col);
     geo->sread_lo[v] = (uint16_t)(row ^ scol(col));
   }
   geo->g7 = (i64)1 << pos[7];
+  geo->g8 = (i64)1 << pos[8];
   for (int r = 0; r < OZ_STEPS; ++r) {
     i64 dep;
     uint32_t row, col;
-    split(r, 8, 4, &dep, &row, &col);
+    split(r, 9, 3, &dep, &row, &col);
     geo->ghi[r] = dep;
     geo->aoff_hi[r] = aoff(row, col);
     geo->sread_hi[r] = (uint16_t)(row ^ scol(col));
@@ -497,8 +629,9 @@ void make_oz_gate(const GateOp& g, const int cbit[5], OzGate* G) {
 
 int* qgb_tc_err_flag();  // qgb_tc.cu
 
-// Uncontrolled 5-qubit dense block on a complex128 state of n >= 12 qubits.
-int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s) {
+// Uncontrolled 5-qubit dense block on a complex128 state of n >= 12 qubits;
+// fix: the state is in the fixed-point format (oz_to_fix).
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix) {
   if (g.tbits.size() != 5 || !g.cbits.empty() || n < 12) {
     qgb_set_error("qgb_apply_fused5_tc: complex128 needs an uncontrolled 5-qubit dense block on >= 12 qubits");
     return QGB_ERR_INVALID;
@@ -510,16 +643,90 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s) {
   int cbit[5];
   make_oz_geom(n, g.tbits, geo, cbit);
   make_oz_gate(g, cbit, G);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_fused5_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-    attr = true;
+  static bool attr[2] = {false, false};
+  if (!attr[fix]) {
+    cudaFuncSetAttribute(fix ? k_fused5_oz<true> : k_fused5_oz<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         OZ_SMEM);
+    attr[fix] = true;
   }
   const i64 ntiles = (i64)1 << (n - 12);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms());
-  k_fused5_oz<<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err);
+  if (fix) k_fused5_oz<true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err);
+  else k_fused5_oz<false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err);
   delete G;
   delete geo;
   QGB_LAUNCH_CHECK("k_fused5_oz");
+  return QGB_OK;
+}
+
+// ---- fixed-point chains of blocks -----------------------------------------
+
+// e with 2^e > 2 ||psi|| from ||psi||^2 (no square root: ||psi|| < 2^ceil(x/2)
+// when ||psi||^2 < 2^x); 0 for the zero state
+__host__ __device__ __forceinline__ int oz_scale_exp(double norm2) {
+  const int x = (int)((oz_dbits(norm2) >> 52) & 0x7FF) - 1022;  // norm2 < 2^x
+  return norm2 > 0 ? ((x + 1) >> 1) + 1 : 0;
+}
+
+__global__ void k_oz_scale(const double* __restrict__ norm2, int* __restrict__ e) { *e = oz_scale_exp(*norm2); }
+
+__global__ void k_oz_to_fix(double2* __restrict__ psi, i64 N, const int* __restrict__ e_ptr) {
+  const int e = *e_ptr;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x) {
+    const double2 v = psi[i];
+    psi[i] = make_double2(oz_bitsd((uint64_t)oz_to_fix(v.x, e)), oz_bitsd((uint64_t)oz_to_fix(v.y, e)));
+  }
+}
+
+__global__ void k_oz_from_fix(double2* __restrict__ psi, i64 N, const int* __restrict__ e_ptr) {
+  const int e = *e_ptr;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x) {
+    const double2 v = psi[i];
+    psi[i] = make_double2(oz_from_fix((int64_t)oz_dbits(v.x), e), oz_from_fix((int64_t)oz_dbits(v.y), e));
+  }
+}
+
+// A block keeps the fixed-point range only if it does not grow the norm:
+// max |(U^dagger U - I)_ij| < 1e-9.
+bool qgb_oz_unitary(const GateOp& g) {
+  for (int i = 0; i < 32; ++i)
+    for (int j = 0; j < 32; ++j) {
+      zd acc = 0;
+      for (int k = 0; k < 32; ++k) acc += std::conj(g.coef[k * 32 + i]) * g.coef[k * 32 + j];
+      if (std::abs(acc - zd(i == j ? 1.0 : 0.0, 0.0)) > 1e-9) return false;
+    }
+  return true;
+}
+
+extern "C" int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scratch, void* stream);
+extern "C" size_t qgb_norm_scratch_bytes(void);
+
+// Consecutive unitary blocks on a complex128 state (n >= 12): the state is
+// converted once to the fixed-point format (scale from its FP64 norm, all on
+// the device), every block runs on it, and it is converted back.  Two extra
+// state passes replace the double <-> digit conversions of every block.
+int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s) {
+  static double* d_norm = nullptr;
+  static int* d_e = nullptr;
+  static void* d_scratch = nullptr;
+  if (!d_norm) {
+    QGB_TRY_CUDA(cudaMalloc(&d_norm, sizeof(double)));
+    QGB_TRY_CUDA(cudaMalloc(&d_e, sizeof(int)));
+    QGB_TRY_CUDA(cudaMalloc(&d_scratch, qgb_norm_scratch_bytes()));
+  }
+  int st = qgb_norm2(state, n, QGB_C128, d_norm, d_scratch, (void*)s);
+  if (st) return st;
+  k_oz_scale<<<1, 1, 0, s>>>(d_norm, d_e);
+  QGB_LAUNCH_CHECK("k_oz_scale");
+  const i64 N = (i64)1 << n;
+  const int grid = (int)std::min<i64>((N + 255) / 256, (i64)qgb_num_sms() * 8);
+  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, d_e);
+  QGB_LAUNCH_CHECK("k_oz_to_fix");
+  for (const GateOp* g : blocks) {
+    st = qgb_launch_fused5_oz(state, n, *g, s, true);
+    if (st) return st;
+  }
+  k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, d_e);
+  QGB_LAUNCH_CHECK("k_oz_from_fix");
   return QGB_OK;
 }

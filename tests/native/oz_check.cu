@@ -12,7 +12,9 @@
 // scales, the worst-case bound of the fixed-point rounding over K = 64), and
 // the largest error over a Gaussian state within 1e-13 of its largest output.
 // Also counts shared-memory wavefronts of the A writes (4-byte) and of the
-// staging writes and reads (16-byte).
+// staging writes and reads (16-byte).  Then replays chains of three unitary
+// blocks in the fixed-point state format (k_fused5_oz<true> between
+// oz_to_fix and oz_from_fix) against the FP64 product.
 // No kernel is launched.
 #include <complex>
 #include <cstdio>
@@ -43,6 +45,169 @@ static int wavefronts(const uint32_t* off, int width) {
     total += m;
   }
   return total;
+}
+
+// One launch of k_fused5_oz<true> replayed on a fixed-point state (X holds
+// the re, im integers of each amplitude): tile shift from the OR of the
+// magnitudes, oz_digits_fix, exact level sums, oz_combine_fix, staging.
+static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, int* exact_fails) {
+  OzGeom* geo = new OzGeom();
+  OzGate* G = new OzGate();
+  int cbit[5];
+  make_oz_geom(n, g.tbits, geo, cbit);
+  make_oz_gate(g, cbit, G);
+  static int Bd[OZ_NSLICE][64][64];
+  for (int nn = 0; nn < 64; ++nn)
+    for (int k = 0; k < 64; ++k) {
+      const int r = nn >> 1, c = k >> 1;
+      const double v = (nn & 1) == 0 ? ((k & 1) == 0 ? G->ur[r][c] : -G->ui[r][c])
+                                     : ((k & 1) == 0 ? G->ui[r][c] : G->ur[r][c]);
+      int d[OZ_NSLICE];
+      oz_digits(v, G->fexp[r], d);
+      for (int j = 0; j < OZ_NSLICE; ++j) Bd[j][nn][k] = d[j];
+    }
+  std::map<uint32_t, std::pair<int, int>> dec;
+  for (int row = 0; row < 128; ++row)
+    for (int c = 0; c < 32; ++c)
+      dec[(c >> 2) * geo->a_lbo + (row >> 3) * OZ_A_SBO + (row & 7) * 16 + (c & 3) * 4] = {row, c};
+  const i64 ntiles = (i64)1 << (n - 12);
+  for (i64 t = 0; t < ntiles; ++t) {
+    const i64 base = host_tile_base(t, *geo);
+    auto gidx = [&](int tid, int r) {
+      return base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
+    };
+    uint64_t o = 0;
+    for (int r = 0; r < OZ_STEPS; ++r)
+      for (int tid = 0; tid < OZ_THREADS; ++tid)
+        for (int part = 0; part < 2; ++part) {
+          const int64_t a = X[2 * gidx(tid, r) + part];
+          o |= (uint64_t)(a < 0 ? -a : a);
+        }
+    const int p = o ? 63 - oz_clz64(o) : -1;
+    const int sh = p > 46 ? p - 46 : 0;
+    static int Ad[OZ_NSLICE][128][64];
+    for (int r = 0; r < OZ_STEPS; ++r)
+      for (int tid = 0; tid < OZ_THREADS; ++tid) {
+        const auto rc = dec[geo->aoff_lo[tid] + geo->aoff_hi[r]];
+        const i64 gi = gidx(tid, r);
+        float fre[OZ_NSLICE], fim[OZ_NSLICE];
+        oz_digits_f(oz_fix47_fix(X[2 * gi], sh), fre);
+        oz_digits_f(oz_fix47_fix(X[2 * gi + 1], sh), fim);
+        int dre[OZ_NSLICE], dim[OZ_NSLICE];
+        for (int s = 0; s < OZ_NSLICE; ++s) {
+          dre[s] = (int)fre[s];
+          dim[s] = (int)fim[s];
+          if ((float)dre[s] != fre[s] || (float)dim[s] != fim[s]) (*exact_fails)++;
+        }
+        for (int s = 0; s < OZ_NSLICE; ++s) {
+          if (std::abs(dre[s]) > 128 || std::abs(dim[s]) > 128) (*exact_fails)++;
+          Ad[s][rc.first][2 * rc.second] = dre[s];
+          Ad[s][rc.first][2 * rc.second + 1] = dim[s];
+        }
+      }
+    std::vector<int64_t> stage(2 * OZ_TILE, 0);
+    for (int row = 0; row < 128; ++row)
+      for (int c = 0; c < 32; ++c)
+        for (int part = 0; part < 2; ++part) {
+          float acc[OZ_NLEVEL];
+          for (int l = 0; l < OZ_NLEVEL; ++l) {
+            int64_t sum = 0;
+            for (int i = std::max(0, l - (OZ_NSLICE - 1)); i <= std::min(l, OZ_NSLICE - 1); ++i)
+              for (int k = 0; k < 64; ++k) sum += (int64_t)Ad[i][row][k] * Bd[l - i][2 * c + part][k];
+            if (std::llabs(sum) >= (1ll << 24)) (*exact_fails)++;
+            acc[l] = (float)sum;
+          }
+          stage[2 * ((uint32_t)row ^ geo->scol[c]) + part] = oz_combine_fix(acc, sh + G->fexp[c] - 1029);
+        }
+    for (int r = 0; r < OZ_STEPS; ++r)
+      for (int tid = 0; tid < OZ_THREADS; ++tid) {
+        const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
+        const i64 gi = gidx(tid, r);
+        X[2 * gi] = stage[2 * si];
+        X[2 * gi + 1] = stage[2 * si + 1];
+      }
+  }
+  delete geo;
+  delete G;
+}
+
+// A chain of three random unitary blocks in the fixed-point format (scale
+// from the FP64 norm, oz_to_fix / oz_from_fix at the ends) against the FP64
+// product: 1e-13 absolute on normalised states, including one whose
+// amplitudes span 2^-30..1.  Returns the number of failures.
+static int chain_check(std::mt19937_64& rng, int* exact_fails) {
+  std::normal_distribution<double> nd;
+  int fails = 0;
+  for (int trial = 0; trial < 4; ++trial) {
+    const int n = 13 + (trial & 1);
+    const i64 N = (i64)1 << n;
+    std::vector<cd> psi(N);
+    double nrm2 = 0;
+    for (auto& x : psi) {
+      x = cd(nd(rng), nd(rng));
+      if (trial >= 2) x *= std::ldexp(1.0, -(int)(rng() % 30));
+      nrm2 += std::norm(x);
+    }
+    for (auto& x : psi) x /= std::sqrt(nrm2);
+    nrm2 = 0;
+    for (auto& x : psi) nrm2 += std::norm(x);
+    const int e = oz_scale_exp(nrm2);
+    std::vector<int64_t> X(2 * N);
+    for (i64 i = 0; i < N; ++i) {
+      X[2 * i] = oz_to_fix(psi[i].real(), e);
+      X[2 * i + 1] = oz_to_fix(psi[i].imag(), e);
+    }
+    std::vector<cd> ref = psi;
+    for (int b = 0; b < 3; ++b) {
+      std::vector<int> all(n);
+      for (int i = 0; i < n; ++i) all[i] = i;
+      std::shuffle(all.begin(), all.end(), rng);
+      GateOp g;
+      g.kind = GK_DENSE;
+      g.tbits.assign(all.begin(), all.begin() + 5);
+      // a random unitary: Gram-Schmidt on a complex Gaussian matrix (columns)
+      std::vector<cd> U(1024);
+      for (auto& u : U) u = cd(nd(rng), nd(rng));
+      for (int j = 0; j < 32; ++j) {
+        for (int k = 0; k < j; ++k) {
+          cd dot = 0;
+          for (int i = 0; i < 32; ++i) dot += std::conj(U[i * 32 + k]) * U[i * 32 + j];
+          for (int i = 0; i < 32; ++i) U[i * 32 + j] -= dot * U[i * 32 + k];
+        }
+        double nn = 0;
+        for (int i = 0; i < 32; ++i) nn += std::norm(U[i * 32 + j]);
+        for (int i = 0; i < 32; ++i) U[i * 32 + j] /= std::sqrt(nn);
+      }
+      g.coef.resize(1024);
+      for (int i = 0; i < 1024; ++i) g.coef[i] = zd(U[i].real(), U[i].imag());
+      if (!qgb_oz_unitary(g)) fails++;
+      replay_fix_block(X, n, g, exact_fails);
+      std::vector<cd> out(N);
+      for (i64 i = 0; i < N; ++i) {
+        int bi = 0;
+        for (int jt = 0; jt < 5; ++jt) bi |= (int)((i >> g.tbits[jt]) & 1) << (4 - jt);
+        if (bi) continue;
+        i64 id[32];
+        for (int q = 0; q < 32; ++q) {
+          id[q] = i;
+          for (int jt = 0; jt < 5; ++jt)
+            if ((q >> (4 - jt)) & 1) id[q] |= (i64)1 << g.tbits[jt];
+        }
+        for (int r = 0; r < 32; ++r) {
+          cd acc = 0;
+          for (int c = 0; c < 32; ++c) acc += U[r * 32 + c] * ref[id[c]];
+          out[id[r]] = acc;
+        }
+      }
+      ref = out;
+    }
+    double err = 0;
+    for (i64 i = 0; i < N; ++i)
+      err = std::max(err, std::abs(cd(oz_from_fix(X[2 * i], e), oz_from_fix(X[2 * i + 1], e)) - ref[i]));
+    printf("fixed-point chain n=%d trial %d: max abs error %.3g\n", n, trial, err);
+    if (err > 1e-13) fails++;
+  }
+  return fails;
 }
 
 int main() {
@@ -122,7 +287,7 @@ int main() {
         int exm = 0;
         for (int r = 0; r < OZ_STEPS; ++r)
           for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             exm = std::max(exm, (int)((oz_dbits(psi[gi].real()) >> 52) & 0x7FF));
             exm = std::max(exm, (int)((oz_dbits(psi[gi].imag()) >> 52) & 0x7FF));
@@ -131,7 +296,7 @@ int main() {
         std::set<uint32_t> used;
         for (int r = 0; r < OZ_STEPS; ++r) {
           for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             seen[gi]++;
             const uint32_t o = geo->aoff_lo[tid] + geo->aoff_hi[r];
@@ -143,7 +308,7 @@ int main() {
             oz_digits(psi[gi].imag(), exm, dim);
             for (int s = 0; s < OZ_NSLICE; ++s) {
               // the packed bf16 pair decodes to the digits
-              const uint32_t w = oz_bf16(dre[s]) | (oz_bf16(dim[s]) << 16);
+              const uint32_t w = oz_pack((float)dre[s], (float)dim[s]);
               uint32_t lo = (w & 0xFFFF) << 16, hi = w & 0xFFFF0000u;
               float flo, fhi;
               memcpy(&flo, &lo, 4);
@@ -192,7 +357,7 @@ int main() {
             }
         for (int r = 0; r < OZ_STEPS; ++r) {
           for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
             if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
@@ -230,6 +395,7 @@ int main() {
     }
   }
   printf("cases %d worst relative error (Gaussian states) %.3g\n", cases, worst);
+  fails += chain_check(rng, &exact_fails);
   printf("index failures %d exactness failures %d bank-pattern failures %d\n", fails, exact_fails, bank_fails);
   return (fails || exact_fails || bank_fails) ? 1 : 0;
 }

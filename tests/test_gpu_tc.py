@@ -141,3 +141,27 @@ def test_fused5_oz_needs_twelve_qubits():
     with pytest.raises(NotImplementedError):
         _lib.check(rt.lib.qgb_apply_fused5_tc(st.ptr, 11, st.code, _lib.int_array((0, 1, 2, 3, 4)),
                                               m.ctypes.data_as(_lib.dp), rt.stream))
+
+
+@pytest.mark.parametrize("scale_last", [1.0, 0.5])
+def test_oz_chain_unnormalised_state(scale_last):
+    """Three blocks through qgb_apply_circuit on a complex128 state of norm
+    7.3.  All unitary: one fixed-point chain whose scale comes from the
+    state's norm.  Last block scaled by 0.5 (not unitary): the run goes
+    through the IEEE-double block path instead.  Both against the FP64
+    oracle, 1e-12 relative to the norm."""
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+
+    n = 13
+    psi = _rand_state(n, 5) * 7.3
+    blocks = [((0, 4, 9, 12, 2), _unitary(41)), ((3, 7, 1, 11, 6), _unitary(42)),
+              ((12, 10, 8, 5, 0), _unitary(43) * scale_last)]
+    b = GB300Backend("complex128")
+    st = DeviceState.from_numpy(psi)
+    b.engine_gb.apply_many(st, [(q, [], u) for q, u in blocks], blocked=True)
+    got = np.asarray(st)
+    want = psi
+    for q, u in blocks:
+        want = ref.apply_gate(want, u, list(q), n)
+    assert np.max(np.abs(got - want)) < 1e-12 * 7.3
