@@ -38,3 +38,4 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);
 int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix);
 bool qgb_oz_unitary(const GateOp& g);
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);
+int qgb_tc_prepare();  // allocate the tensor-core paths' device buffers (idempotent)

@@ -41,6 +41,8 @@ int qgb_num_sms() {
   return g_sms;
 }
 
+int qgb_tc_prepare();  // qgb_tc128.cu: tensor-core device buffers
+
 extern "C" {
 
 const char* qgb_last_error(void) { return g_err; }
@@ -51,6 +53,8 @@ int qgb_device_init(int device, int* sm_count) {
   QGB_TRY_CUDA(cudaSetDevice(device));
   QGB_TRY_CUDA(cudaFree(0));  // create the primary context
   g_sms = 0;
+  int st = qgb_tc_prepare();
+  if (st) return st;
   if (sm_count) *sm_count = qgb_num_sms();
   return QGB_OK;
 }

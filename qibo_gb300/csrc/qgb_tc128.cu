@@ -34,13 +34,19 @@
 // per tile.
 //
 // A CTA (512 threads, one per SM: 223 KB of shared memory, 448 TMEM columns)
-// owns 4096-amplitude tiles with the index geometry of qgb_tc.cu (thread t
-// moves amplitudes t + 512 r, r < 8); the next tile is prefetched into
-// registers while the MMAs run.  The digit split and the combination are
-// integer work on the ALU pipe; 16 warps keep it issuing.  The wait on the
-// mbarrier is bounded: on timeout the kernel records an error flag, waits
-// once more (bounded) for the in-flight MMAs, frees its tensor memory and
-// returns.
+// owns 4096-amplitude tiles with the index geometry of qgb_tc.cu.  Warps 0-7
+// convert (thread t moves amplitudes t + 256 r, r < 16, prefetched into
+// registers while the previous MMAs run) and issue the MMAs; warps 8-15 read
+// the levels from TMEM, combine and store, overlapping the conversion of the
+// next tile.  The digit split runs on the FMA pipe (exact FP32 arithmetic
+// on 16-bit chunks), the level combination as an integer multiply-add chain.
+// Every wait on an mbarrier is bounded: on timeout the kernel records an
+// error flag, both groups stop at their next check, the converter waits once
+// more (bounded) for its in-flight MMAs, and tensor memory is freed.
+//
+// Runs of unitary blocks (qgb_run_oz_chain) keep the state in a 64-bit
+// fixed-point format between blocks (k_fused5_oz<true>), converted from and
+// back to IEEE doubles once per run.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -49,8 +55,9 @@
 #include "qgb_plan.h"
 #include "qgb_tcgen05.cuh"
 
-#define OZ_THREADS 512
-#define OZ_STEPS 8     // amplitudes per thread per tile
+#define OZ_THREADS 512  // 8 converter warps + 8 epilogue warps
+#define OZ_GROUP 256    // threads per group
+#define OZ_STEPS 16     // amplitudes per group thread per tile
 #define OZ_TILE 4096   // amplitudes per tile
 #define OZ_NSLICE 6    // digits per value
 #define OZ_NLEVEL 7    // digit-product levels kept (i + j <= 6)
@@ -71,12 +78,12 @@
 
 static_assert(OZ_OFF_B % 16 == 0 && OZ_OFF_STAGE % 16 == 0, "operand regions 16-byte aligned");
 static_assert(OZ_SMEM <= 227 * 1024, "one CTA per SM");
-static_assert(OZ_THREADS * OZ_STEPS == OZ_TILE, "one amplitude per thread and step");
+static_assert(OZ_GROUP * OZ_STEPS == OZ_TILE, "one amplitude per group thread and step");
 
 // Tile geometry (the tile of the complex64 kernel): tile index
-// j = t + 512 r has global offset base + (t & 127) + t7 g7 + t8 g8 + ghi[r]
-// (t7, t8 bits 7 and 8 of t); its (re, im) bf16 pair sits at byte
-// aoff_lo[t] + aoff_hi[r] of
+// j = t + 256 r (t a thread of either group) has global offset
+// base + (t & 127) + t7 g7 + ghi[r] (t7 bit 7 of t); its (re, im) bf16 pair
+// sits at byte aoff_lo[t] + aoff_hi[r] of
 // every A slice; staging slot of (row, column c) is
 //   (c << 7 | row) ^ ((c << g3) & 7),   g3 = 3 - (block qubits on bits 0..2),
 // written as row ^ scol[c] and read as sread_lo[t] ^ sread_hi[r].
@@ -84,11 +91,11 @@ struct OzGeom {
   int nrest;
   int rest[32];
   uint32_t a_lbo;
-  i64 g7, g8;
+  i64 g7;
   i64 ghi[OZ_STEPS];
-  uint32_t aoff_lo[OZ_THREADS];
+  uint32_t aoff_lo[OZ_GROUP];
   uint32_t aoff_hi[OZ_STEPS];
-  uint16_t sread_lo[OZ_THREADS];
+  uint16_t sread_lo[OZ_GROUP];
   uint16_t sread_hi[OZ_STEPS];
   uint16_t scol[32];
 };
@@ -317,20 +324,38 @@ __device__ __forceinline__ void oz_mma(uint32_t d, uint64_t a, uint64_t b, uint3
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
+__device__ __forceinline__ void oz_bar(int id) { asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(OZ_GROUP) : "memory"); }
+
+__device__ __forceinline__ void oz_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+
 // FIX: the state holds fixed-point integers (oz_to_fix) instead of IEEE
 // doubles; the tile scale is then a shift and the output a rounding shift.
+//
+// Warps 0-7 convert: tile scale, digits into the A slices, and thread 0
+// issues the tile's MMAs.  Warps 8-15 read the level accumulators from
+// TMEM, combine them, stage and store the tile.  The converters of tile
+// i + 1 run while the epilogue of tile i runs, and the epilogue's stores
+// overlap the MMAs of tile i + 1.  Handoffs (each completes once per tile,
+// and no waiter can fall two phases behind):
+//   mb_full  (tcgen05.commit)       MMAs of tile i done: A free, TMEM ready
+//   mb_tfree (epilogue thread 0)    TMEM of tile i read: MMAs of i + 1 may start
+//   mb_scale (converter thread 0)   the scale of tile i is in tile_scale[i & 1]
 template <bool FIX>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_fused5_oz(double2* __restrict__ psi, i64 ntiles, const __grid_constant__ OzGeom geo,
                 const __grid_constant__ OzGate G, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mb_full, mb_tfree, mb_scale;
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag;
-  __shared__ uint32_t red[OZ_THREADS / 32], red_hi[OZ_THREADS / 32];
+  __shared__ int abort_flag;      // set by either group on a failed wait
+  __shared__ int c_stop, e_stop;  // each group's decision, written by its thread 0 before its barrier
+  __shared__ uint32_t red[OZ_GROUP / 32], red_hi[OZ_GROUP / 32];
+  __shared__ int tile_scale[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t s_base = smem_u32(sm);
-  const uint32_t mb = smem_u32(&mbar);
+  const uint32_t mfull = smem_u32(&mb_full), mtfree = smem_u32(&mb_tfree), mscale = smem_u32(&mb_scale);
 
   // B slices: stacked row 64 j + n holds digit j of realified row n
   // (n = 2 r + re/im of output r), column k = 2 c + re/im of input c
@@ -346,7 +371,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   }
   if (tid == 0) {
     abort_flag = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mfull));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mtfree));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mscale));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
@@ -358,165 +385,191 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_base;
-  uint32_t phase = 0;
-  const uint32_t aoff = geo.aoff_lo[tid];
-  const uint32_t srd = geo.sread_lo[tid];
   const uint32_t a_lbo = geo.a_lbo;
   const int my_rest = lane < geo.nrest ? geo.rest[lane] : -1;
-  const i64 toff = (i64)(tid & 127) + (((tid >> 7) & 1) ? geo.g7 : 0) + ((tid >> 8) ? geo.g8 : 0);
-  double2* stage = (double2*)(sm + OZ_OFF_STAGE);
-  // epilogue: this warp's TMEM sub-partition (group rows) and column quarter
-  const int erow = 32 * (warp & 3) + lane;
-  const int equart = warp >> 2;
-  const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+  const int g = tid & (OZ_GROUP - 1);  // thread within its group
+  const i64 toff = (i64)(g & 127) + ((g >> 7) ? geo.g7 : 0);
 
-  double2 v[OZ_STEPS];
-  i64 t = blockIdx.x;
-  i64 base = 0;
-  if (t < ntiles) {
-    base = tile_base(t, lane, my_rest);
-    const double2* src = psi + base + toff;
-#pragma unroll
-    for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
-  }
-  for (; t < ntiles; t += gridDim.x) {
-    // tile scale: doubles -- the largest biased exponent among the tile's
-    // 8192 values; fixed point -- the top bit of the OR of their magnitudes
-    int exm = 0, sh = 0;
-    if (FIX) {
-      uint64_t o = 0;
-#pragma unroll
-      for (int r = 0; r < OZ_STEPS; ++r) {
-        const int64_t a = (int64_t)oz_dbits(v[r].x), b = (int64_t)oz_dbits(v[r].y);
-        o |= (uint64_t)(a < 0 ? -a : a) | (uint64_t)(b < 0 ? -b : b);
-      }
-      const uint32_t olo = __reduce_or_sync(0xffffffffu, (uint32_t)o);
-      const uint32_t ohi = __reduce_or_sync(0xffffffffu, (uint32_t)(o >> 32));
-      if (lane == 0) {
-        red[warp] = olo;
-        red_hi[warp] = ohi;
-      }
-      __syncthreads();
-      uint64_t ot = 0;
-#pragma unroll
-      for (int w = 0; w < OZ_THREADS / 32; ++w) ot |= ((uint64_t)red_hi[w] << 32) | red[w];
-      const int p = ot ? 63 - oz_clz64(ot) : -1;
-      sh = p > 46 ? p - 46 : 0;
-    } else {
-      uint32_t m = 0;
-#pragma unroll
-      for (int r = 0; r < OZ_STEPS; ++r) {
-        m = max(m, (uint32_t)(oz_dbits(v[r].x) >> 32) & 0x7FF00000u);
-        m = max(m, (uint32_t)(oz_dbits(v[r].y) >> 32) & 0x7FF00000u);
-      }
-      m = __reduce_max_sync(0xffffffffu, m);
-      if (lane == 0) red[warp] = m;
-      __syncthreads();
-      uint32_t mx = red[0];
-#pragma unroll
-      for (int w = 1; w < OZ_THREADS / 32; ++w) mx = max(mx, red[w]);
-      exm = (int)(mx >> 20);
-    }
-    // digits -> A slices (one (re, im) bf16 pair per slice and amplitude)
-#pragma unroll
-    for (int r = 0; r < OZ_STEPS; ++r) {
-      float dre[OZ_NSLICE], dim[OZ_NSLICE];
-      if (FIX) {
-        oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].x), sh), dre);
-        oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].y), sh), dim);
-      } else {
-        oz_digits_f(oz_fix47(v[r].x, exm), dre);
-        oz_digits_f(oz_fix47(v[r].y, exm), dim);
-      }
-      unsigned char* a = sm + OZ_OFF_A + aoff + geo.aoff_hi[r];
-#pragma unroll
-      for (int s = 0; s < OZ_NSLICE; ++s) *(uint32_t*)(a + s * OZ_A_SLICE) = oz_pack(dre[s], dim[s]);
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {  // K-steps of 16
-        const uint32_t bs = s_base + OZ_OFF_B + s * 2 * OZ_B_LBO;
-        const uint64_t b0 = smem_desc(bs, OZ_B_LBO, OZ_B_SBO);                    // B rows 0..
-        const uint64_t b256 = smem_desc(bs + 32 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 256..
-        const uint64_t b320 = smem_desc(bs + 40 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 320..
-#pragma unroll
-        for (int i = 0; i < OZ_NSLICE; ++i) {
-          const uint64_t adesc = smem_desc(s_base + OZ_OFF_A + i * OZ_A_SLICE + s * 2 * a_lbo, a_lbo, OZ_A_SBO);
-          const int nrows = 64 * (i <= 1 ? OZ_NSLICE : OZ_NLEVEL - i);  // B slices 0..min(5, 6 - i)
-          const uint32_t acc = (i > 0 || s > 0) ? 1u : 0u;
-          if (s == 0 && i == 1) {
-            // levels 1..5 accumulate onto slice 0's products; level 6 starts here
-            oz_mma(tmem + 64, adesc, b0, oz_idesc(256), 1u);
-            oz_mma(tmem + 64 + 256, adesc, b256, oz_idesc(64), 1u);
-            oz_mma(tmem + 64 + 320, adesc, b320, oz_idesc(64), 0u);
-          } else {
-            oz_mma(tmem + 64 * i, adesc, b0, oz_idesc(nrows < 256 ? nrows : 256), acc);
-            if (nrows > 256) oz_mma(tmem + 64 * i + 256, adesc, b256, oz_idesc(nrows - 256), acc);
-          }
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
-                   : "memory");
-    }
-    // prefetch the next tile into registers while the MMAs run
-    const i64 tn = t + gridDim.x;
-    i64 nbase = 0;
-    if (tn < ntiles) {
-      nbase = tile_base(tn, lane, my_rest);
-      const double2* src = psi + nbase + toff;
+  if (warp < OZ_GROUP / 32) {
+    // ---------------------------------------------------------- converters
+    const uint32_t aoff = geo.aoff_lo[g];
+    double2 v[OZ_STEPS];
+    i64 t = blockIdx.x;
+    if (t < ntiles) {
+      const double2* src = psi + tile_base(t, lane, my_rest) + toff;
 #pragma unroll
       for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
     }
-    // one thread waits for the MMAs; the rest park at the barrier
-    if (tid == 0 && !mbar_wait(mb, phase)) abort_flag = 1;
-    __syncthreads();
-    if (abort_flag) {
-      // record the failure, give the in-flight MMAs one more bounded wait so
-      // tensor memory is not freed under them, then leave
-      if (tid == 0) {
-        atomicExch(err, 1);
-        mbar_wait(mb, phase);
-      }
-      break;
-    }
-    phase ^= 1;
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // epilogue: combine the seven levels of 8 reals (4 amplitudes) at a time
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-      float acc[OZ_NLEVEL][8];
+    int it = 0;
+    bool pending = false;  // thread 0: MMAs issued whose completion it has not seen
+    for (; t < ntiles; t += gridDim.x, ++it) {
+      // tile scale: doubles -- the largest biased exponent among the tile's
+      // 8192 values; fixed point -- the top bit of the OR of their magnitudes
+      uint32_t m = 0, mh = 0;
+      if (FIX) {
+        uint64_t o = 0;
 #pragma unroll
-      for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(trow + 64 * l + 16 * equart + 8 * h, acc[l]);
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-      for (int e = 0; e < 8; e += 2) {
-        const int c = 8 * equart + 4 * h + (e >> 1);  // output amplitude (permuted block index)
-        float are[OZ_NLEVEL], aim[OZ_NLEVEL];
-#pragma unroll
-        for (int l = 0; l < OZ_NLEVEL; ++l) {
-          are[l] = acc[l][e];
-          aim[l] = acc[l][e + 1];
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          const int64_t a = (int64_t)oz_dbits(v[r].x), b = (int64_t)oz_dbits(v[r].y);
+          o |= (uint64_t)(a < 0 ? -a : a) | (uint64_t)(b < 0 ? -b : b);
         }
+        m = __reduce_or_sync(0xffffffffu, (uint32_t)o);
+        mh = __reduce_or_sync(0xffffffffu, (uint32_t)(o >> 32));
+      } else {
+#pragma unroll
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          m = max(m, (uint32_t)(oz_dbits(v[r].x) >> 32) & 0x7FF00000u);
+          m = max(m, (uint32_t)(oz_dbits(v[r].y) >> 32) & 0x7FF00000u);
+        }
+        m = __reduce_max_sync(0xffffffffu, m);
+      }
+      if (lane == 0) {
+        red[warp] = m;
+        red_hi[warp] = mh;
+      }
+      // the A slices are free once the MMAs of the previous tile are done
+      if (g == 0) {
+        bool bad = abort_flag != 0;
+        if (!bad && pending) {
+          if (mbar_wait(mfull, (uint32_t)(it - 1) & 1)) pending = false;
+          else bad = true;
+        }
+        if (bad) abort_flag = 1;
+        c_stop = bad;
+      }
+      oz_bar(1);
+      if (c_stop) break;
+      int scale;  // exm (doubles) or sh (fixed point)
+      if (FIX) {
+        uint64_t ot = 0;
+#pragma unroll
+        for (int w = 0; w < OZ_GROUP / 32; ++w) ot |= ((uint64_t)red_hi[w] << 32) | red[w];
+        const int p = ot ? 63 - oz_clz64(ot) : -1;
+        scale = p > 46 ? p - 46 : 0;
+      } else {
+        uint32_t mx = red[0];
+#pragma unroll
+        for (int w = 1; w < OZ_GROUP / 32; ++w) mx = max(mx, red[w]);
+        scale = (int)(mx >> 20);
+      }
+      // digits -> A slices (one (re, im) bf16 pair per slice and amplitude)
+#pragma unroll
+      for (int r = 0; r < OZ_STEPS; ++r) {
+        float dre[OZ_NSLICE], dim[OZ_NSLICE];
         if (FIX) {
-          const int k = sh + G.fexp[c] - 1029;
-          stage[erow ^ geo.scol[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
-                                                   oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
+          oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].x), scale), dre);
+          oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].y), scale), dim);
         } else {
-          const int sc = exm + G.fexp[c] - 2098;
-          stage[erow ^ geo.scol[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+          oz_digits_f(oz_fix47(v[r].x, scale), dre);
+          oz_digits_f(oz_fix47(v[r].y, scale), dim);
+        }
+        unsigned char* a = sm + OZ_OFF_A + aoff + geo.aoff_hi[r];
+#pragma unroll
+        for (int s = 0; s < OZ_NSLICE; ++s) *(uint32_t*)(a + s * OZ_A_SLICE) = oz_pack(dre[s], dim[s]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      oz_bar(1);
+      if (g == 0) {
+        // the MMAs overwrite TMEM: wait until the epilogue has read tile it - 1
+        bool ok = it == 0 || mbar_wait(mtfree, (uint32_t)(it - 1) & 1);
+        if (ok) {
+          tile_scale[it & 1] = scale;
+          oz_arrive(mscale);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {  // K-steps of 16
+            const uint32_t bs = s_base + OZ_OFF_B + s * 2 * OZ_B_LBO;
+            const uint64_t b0 = smem_desc(bs, OZ_B_LBO, OZ_B_SBO);                    // B rows 0..
+            const uint64_t b256 = smem_desc(bs + 32 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 256..
+            const uint64_t b320 = smem_desc(bs + 40 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 320..
+#pragma unroll
+            for (int i = 0; i < OZ_NSLICE; ++i) {
+              const uint64_t adesc = smem_desc(s_base + OZ_OFF_A + i * OZ_A_SLICE + s * 2 * a_lbo, a_lbo, OZ_A_SBO);
+              const int nrows = 64 * (i <= 1 ? OZ_NSLICE : OZ_NLEVEL - i);  // B slices 0..min(5, 6 - i)
+              const uint32_t acc = (i > 0 || s > 0) ? 1u : 0u;
+              if (s == 0 && i == 1) {
+                // levels 1..5 accumulate onto slice 0's products; level 6 starts here
+                oz_mma(tmem + 64, adesc, b0, oz_idesc(256), 1u);
+                oz_mma(tmem + 64 + 256, adesc, b256, oz_idesc(64), 1u);
+                oz_mma(tmem + 64 + 320, adesc, b320, oz_idesc(64), 0u);
+              } else {
+                oz_mma(tmem + 64 * i, adesc, b0, oz_idesc(nrows < 256 ? nrows : 256), acc);
+                if (nrows > 256) oz_mma(tmem + 64 * i + 256, adesc, b256, oz_idesc(nrows - 256), acc);
+              }
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mfull)
+                       : "memory");
+          pending = true;
+        } else {
+          abort_flag = 1;
         }
       }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    double2* dst = psi + base + toff;
+      // prefetch the next tile into registers while the MMAs run
+      const i64 tn = t + gridDim.x;
+      if (tn < ntiles) {
+        const double2* src = psi + tile_base(tn, lane, my_rest) + toff;
 #pragma unroll
-    for (int r = 0; r < OZ_STEPS; ++r) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
-    base = nbase;
+        for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
+      }
+    }
+    // on an abort, give the last issued MMAs one more bounded wait so that
+    // tensor memory is not freed under them
+    if (g == 0 && pending) mbar_wait(mfull, (uint32_t)(it - 1) & 1);
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int ew = warp - OZ_GROUP / 32;  // TMEM sub-partition ew & 3, column half ew >> 2
+    const int erow = 32 * (ew & 3) + lane;
+    const int ehalf = ew >> 2;
+    const uint32_t trow = tmem + ((uint32_t)(32 * (ew & 3)) << 16);
+    const uint32_t srd = geo.sread_lo[g];
+    double2* stage = (double2*)(sm + OZ_OFF_STAGE);
+    int it = 0;
+    for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+      if (g == 0) {
+        const uint32_t par = (uint32_t)it & 1;
+        const bool bad = abort_flag || !mbar_wait(mscale, par) || !mbar_wait(mfull, par);
+        if (bad) abort_flag = 1;
+        e_stop = bad;
+      }
+      oz_bar(2);
+      if (e_stop) break;
+      const int scale = tile_scale[it & 1];
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      // combine the seven levels of 8 reals (4 amplitudes) at a time
+#pragma unroll 1
+      for (int q = 0; q < 4; ++q) {
+        float acc[OZ_NLEVEL][8];
+#pragma unroll
+        for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(trow + 64 * l + 32 * ehalf + 8 * q, acc[l]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const int c = 16 * ehalf + 4 * q + (e >> 1);  // output amplitude (permuted block index)
+          float are[OZ_NLEVEL], aim[OZ_NLEVEL];
+#pragma unroll
+          for (int l = 0; l < OZ_NLEVEL; ++l) {
+            are[l] = acc[l][e];
+            aim[l] = acc[l][e + 1];
+          }
+          if (FIX) {
+            const int k = scale + G.fexp[c] - 1029;
+            stage[erow ^ geo.scol[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
+                                                     oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
+          } else {
+            const int sc = scale + G.fexp[c] - 2098;
+            stage[erow ^ geo.scol[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      oz_bar(2);
+      if (g == 0) oz_arrive(mtfree);  // TMEM of this tile read: the next MMAs may start
+      // store the tile (overlaps the next tile's MMAs)
+      double2* dst = psi + tile_base(t, lane, my_rest) + toff;
+#pragma unroll
+      for (int r = 0; r < OZ_STEPS; ++r) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
+    }
   }
   __syncthreads();
   if (warp == 0)
@@ -581,19 +634,18 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
       else *col |= 1u << colbit[b];
     }
   };
-  for (int v = 0; v < OZ_THREADS; ++v) {
+  for (int v = 0; v < OZ_GROUP; ++v) {
     i64 dep;
     uint32_t row, col;
-    split(v, 0, 9, &dep, &row, &col);
+    split(v, 0, 8, &dep, &row, &col);
     geo->aoff_lo[v] = aoff(row, col);
     geo->sread_lo[v] = (uint16_t)(row ^ scol(col));
   }
   geo->g7 = (i64)1 << pos[7];
-  geo->g8 = (i64)1 << pos[8];
   for (int r = 0; r < OZ_STEPS; ++r) {
     i64 dep;
     uint32_t row, col;
-    split(r, 9, 3, &dep, &row, &col);
+    split(r, 8, 4, &dep, &row, &col);
     geo->ghi[r] = dep;
     geo->aoff_hi[r] = aoff(row, col);
     geo->sread_hi[r] = (uint16_t)(row ^ scol(col));
@@ -701,32 +753,45 @@ bool qgb_oz_unitary(const GateOp& g) {
 extern "C" int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scratch, void* stream);
 extern "C" size_t qgb_norm_scratch_bytes(void);
 
+namespace {
+double* g_oz_norm = nullptr;  // chain scratch: ||psi||^2, the scale e, the norm reduction
+int* g_oz_e = nullptr;
+void* g_oz_scratch = nullptr;
+}  // namespace
+
+// Device buffers of the tensor-core paths (error flag, chain scratch),
+// allocated once; called by qgb_device_init so that a stream capture of
+// qgb_apply_circuit finds them in place.
+int qgb_tc_prepare() {
+  if (!qgb_tc_err_flag()) return QGB_ERR_CUDA;
+  if (!g_oz_norm) {
+    QGB_TRY_CUDA(cudaMalloc(&g_oz_norm, sizeof(double)));
+    QGB_TRY_CUDA(cudaMalloc(&g_oz_e, sizeof(int)));
+    QGB_TRY_CUDA(cudaMalloc(&g_oz_scratch, qgb_norm_scratch_bytes()));
+  }
+  return QGB_OK;
+}
+
 // Consecutive unitary blocks on a complex128 state (n >= 12): the state is
 // converted once to the fixed-point format (scale from its FP64 norm, all on
 // the device), every block runs on it, and it is converted back.  Two extra
 // state passes replace the double <-> digit conversions of every block.
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s) {
-  static double* d_norm = nullptr;
-  static int* d_e = nullptr;
-  static void* d_scratch = nullptr;
-  if (!d_norm) {
-    QGB_TRY_CUDA(cudaMalloc(&d_norm, sizeof(double)));
-    QGB_TRY_CUDA(cudaMalloc(&d_e, sizeof(int)));
-    QGB_TRY_CUDA(cudaMalloc(&d_scratch, qgb_norm_scratch_bytes()));
-  }
-  int st = qgb_norm2(state, n, QGB_C128, d_norm, d_scratch, (void*)s);
+  int st = qgb_tc_prepare();
   if (st) return st;
-  k_oz_scale<<<1, 1, 0, s>>>(d_norm, d_e);
+  st = qgb_norm2(state, n, QGB_C128, g_oz_norm, g_oz_scratch, (void*)s);
+  if (st) return st;
+  k_oz_scale<<<1, 1, 0, s>>>(g_oz_norm, g_oz_e);
   QGB_LAUNCH_CHECK("k_oz_scale");
   const i64 N = (i64)1 << n;
   const int grid = (int)std::min<i64>((N + 255) / 256, (i64)qgb_num_sms() * 8);
-  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, d_e);
+  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, g_oz_e);
   QGB_LAUNCH_CHECK("k_oz_to_fix");
   for (const GateOp* g : blocks) {
     st = qgb_launch_fused5_oz(state, n, *g, s, true);
     if (st) return st;
   }
-  k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, d_e);
+  k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, g_oz_e);
   QGB_LAUNCH_CHECK("k_oz_from_fix");
   return QGB_OK;
 }

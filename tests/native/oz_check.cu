@@ -74,11 +74,11 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
   for (i64 t = 0; t < ntiles; ++t) {
     const i64 base = host_tile_base(t, *geo);
     auto gidx = [&](int tid, int r) {
-      return base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
+      return base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
     };
     uint64_t o = 0;
     for (int r = 0; r < OZ_STEPS; ++r)
-      for (int tid = 0; tid < OZ_THREADS; ++tid)
+      for (int tid = 0; tid < OZ_GROUP; ++tid)
         for (int part = 0; part < 2; ++part) {
           const int64_t a = X[2 * gidx(tid, r) + part];
           o |= (uint64_t)(a < 0 ? -a : a);
@@ -87,7 +87,7 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
     const int sh = p > 46 ? p - 46 : 0;
     static int Ad[OZ_NSLICE][128][64];
     for (int r = 0; r < OZ_STEPS; ++r)
-      for (int tid = 0; tid < OZ_THREADS; ++tid) {
+      for (int tid = 0; tid < OZ_GROUP; ++tid) {
         const auto rc = dec[geo->aoff_lo[tid] + geo->aoff_hi[r]];
         const i64 gi = gidx(tid, r);
         float fre[OZ_NSLICE], fim[OZ_NSLICE];
@@ -120,7 +120,7 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
           stage[2 * ((uint32_t)row ^ geo->scol[c]) + part] = oz_combine_fix(acc, sh + G->fexp[c] - 1029);
         }
     for (int r = 0; r < OZ_STEPS; ++r)
-      for (int tid = 0; tid < OZ_THREADS; ++tid) {
+      for (int tid = 0; tid < OZ_GROUP; ++tid) {
         const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
         const i64 gi = gidx(tid, r);
         X[2 * gi] = stage[2 * si];
@@ -286,8 +286,8 @@ int main() {
         const i64 base = host_tile_base(t, *geo);
         int exm = 0;
         for (int r = 0; r < OZ_STEPS; ++r)
-          for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
+          for (int tid = 0; tid < OZ_GROUP; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             exm = std::max(exm, (int)((oz_dbits(psi[gi].real()) >> 52) & 0x7FF));
             exm = std::max(exm, (int)((oz_dbits(psi[gi].imag()) >> 52) & 0x7FF));
@@ -295,8 +295,8 @@ int main() {
         static int Ad[OZ_NSLICE][128][64];
         std::set<uint32_t> used;
         for (int r = 0; r < OZ_STEPS; ++r) {
-          for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
+          for (int tid = 0; tid < OZ_GROUP; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             seen[gi]++;
             const uint32_t o = geo->aoff_lo[tid] + geo->aoff_hi[r];
@@ -320,7 +320,7 @@ int main() {
             }
           }
           if (t == 0)
-            for (int w = 0; w < OZ_THREADS / 32; ++w) {
+            for (int w = 0; w < OZ_GROUP / 32; ++w) {
               uint32_t off[32];
               for (int l = 0; l < 32; ++l) off[l] = geo->aoff_lo[32 * w + l] + geo->aoff_hi[r];
               if (wavefronts(off, 4) > (t5 >= 2 ? 1 : t5 == 1 ? 2 : 4)) bank_fails++;
@@ -356,8 +356,8 @@ int main() {
               if (wavefronts(off, 16) > 4) bank_fails++;
             }
         for (int r = 0; r < OZ_STEPS; ++r) {
-          for (int tid = 0; tid < OZ_THREADS; ++tid) {
-            const i64 gi = base + (tid & 127) + (((tid >> 7) & 1) ? geo->g7 : 0) + ((tid >> 8) ? geo->g8 : 0) + geo->ghi[r];
+          for (int tid = 0; tid < OZ_GROUP; ++tid) {
+            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
             if (gi < 0 || gi >= N) { bad = true; continue; }
             const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
             if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
@@ -366,7 +366,7 @@ int main() {
             bound[gi] = bstage[si];
           }
           if (t == 0)
-            for (int w = 0; w < OZ_THREADS / 32; ++w) {
+            for (int w = 0; w < OZ_GROUP / 32; ++w) {
               uint32_t off[32];
               for (int l = 0; l < 32; ++l) off[l] = 16 * ((uint32_t)geo->sread_lo[32 * w + l] ^ geo->sread_hi[r]);
               if (wavefronts(off, 16) > 4) bank_fails++;
