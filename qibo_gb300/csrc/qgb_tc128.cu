@@ -73,20 +73,19 @@
 #define OZ_B_LBO (OZ_B_ROWS / 8 * OZ_B_SBO)  // 6144
 #define OZ_OFF_A 0
 #define OZ_OFF_B (OZ_OFF_A + OZ_NSLICE * OZ_A_SLICE)  // 113664
-#define OZ_OFF_STAGE (OZ_OFF_B + 8 * OZ_B_LBO)        // 162816
-#define OZ_SMEM (OZ_OFF_STAGE + OZ_TILE * 16)         // 228352
+#define OZ_SMEM (OZ_OFF_B + 8 * OZ_B_LBO)             // 162816
 
-static_assert(OZ_OFF_B % 16 == 0 && OZ_OFF_STAGE % 16 == 0, "operand regions 16-byte aligned");
+static_assert(OZ_OFF_B % 16 == 0, "operand regions 16-byte aligned");
 static_assert(OZ_SMEM <= 227 * 1024, "one CTA per SM");
 static_assert(OZ_GROUP * OZ_STEPS == OZ_TILE, "one amplitude per group thread and step");
 
-// Tile geometry (the tile of the complex64 kernel): tile index
-// j = t + 256 r (t a thread of either group) has global offset
-// base + (t & 127) + t7 g7 + ghi[r] (t7 bit 7 of t); its (re, im) bf16 pair
-// sits at byte aoff_lo[t] + aoff_hi[r] of
-// every A slice; staging slot of (row, column c) is
-//   (c << 7 | row) ^ ((c << g3) & 7),   g3 = 3 - (block qubits on bits 0..2),
-// written as row ^ scol[c] and read as sread_lo[t] ^ sread_hi[r].
+// Tile geometry (the tile of the complex64 kernel).  Loads: tile index
+// j = t + 256 r (t a converter thread) has global offset base + (t & 127) +
+// t7 g7 + ghi[r] (t7 bit 7 of t); its (re, im) bf16 pair sits at byte
+// aoff_lo[t] + aoff_hi[r] of every A slice.  Stores: output (group row,
+// permuted block column c) goes to base + rowoff[row] + coloff[c], straight
+// from the epilogue's registers (a warp's lanes are consecutive rows, i.e.
+// the tile's lowest non-block index bits).
 struct OzGeom {
   int nrest;
   int rest[32];
@@ -95,9 +94,8 @@ struct OzGeom {
   i64 ghi[OZ_STEPS];
   uint32_t aoff_lo[OZ_GROUP];
   uint32_t aoff_hi[OZ_STEPS];
-  uint16_t sread_lo[OZ_GROUP];
-  uint16_t sread_hi[OZ_STEPS];
-  uint16_t scol[32];
+  i64 rowoff[128];
+  i64 coloff[32];
 };
 
 // The (permuted) block in FP64 and, per output row r, the biased exponent of
@@ -274,12 +272,25 @@ __host__ __device__ __forceinline__ double oz_combine(const float acc[OZ_NLEVEL]
   return oz_i64_to_double(oz_levels(acc), sc);
 }
 
-// round(T * 2^k) as a 64-bit integer (fixed-point output; |result| < 2^62)
-__host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NLEVEL], int k) {
-  const int64_t T = oz_levels(acc);
-  if (k >= 0) return T * ((int64_t)1 << k);
-  if (k <= -63) return 0;
-  return (T + ((int64_t)1 << (-k - 1))) >> (-k);
+// Shift amounts of round(T 2^k) without branches (one pair per output
+// column, shared by its real and imaginary parts): lsh = max(k, 0),
+// rsh = min(max(-k, 0), 62) (a shift by 62 already rounds every |T| < 2^61
+// to 0).
+struct OzShift {
+  int lsh, rsh;
+};
+__host__ __device__ __forceinline__ OzShift oz_shift(int k) {
+  OzShift r;
+  r.lsh = k > 0 ? k : 0;
+  r.rsh = k < 0 ? (k > -62 ? -k : 62) : 0;
+  return r;
+}
+
+// round(T * 2^k) as a 64-bit integer (fixed-point output; |result| < 2^62),
+// straight-line code
+__host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NLEVEL], OzShift sh) {
+  const int64_t t = (int64_t)((uint64_t)oz_levels(acc) << sh.lsh);
+  return (t + (((int64_t)1 << sh.rsh) >> 1)) >> sh.rsh;
 }
 
 // Fixed-point state format between consecutive tensor-core blocks: a real
@@ -304,7 +315,7 @@ __host__ __device__ __forceinline__ double oz_from_fix(int64_t X, int e) { retur
 // 47-bit value of a fixed-point X at tile shift sh (the tile's largest |X|
 // is below 2^(47 + sh)), rounding half up
 __host__ __device__ __forceinline__ int64_t oz_fix47_fix(int64_t X, int sh) {
-  return sh > 0 ? (X + ((int64_t)1 << (sh - 1))) >> sh : X;
+  return (X + (((int64_t)1 << sh) >> 1)) >> sh;  // sh >= 0; no rounding term for sh = 0
 }
 
 // byte offset of element (row, k) of the stacked B slices (dense, K-major)
@@ -335,7 +346,7 @@ __device__ __forceinline__ void oz_arrive(uint32_t mbar) {
 //
 // Warps 0-7 convert: tile scale, digits into the A slices, and thread 0
 // issues the tile's MMAs.  Warps 8-15 read the level accumulators from
-// TMEM, combine them, stage and store the tile.  The converters of tile
+// TMEM, combine them and store them straight to the state.  The converters of tile
 // i + 1 run while the epilogue of tile i runs, and the epilogue's stores
 // overlap the MMAs of tile i + 1.  Handoffs (each completes once per tile,
 // and no waiter can fall two phases behind):
@@ -469,6 +480,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       oz_bar(1);
+      // prefetch the next tile into registers (the digits are in shared
+      // memory now); issued before the MMAs, whose issue blocks thread 0 and
+      // with it the rest of warp 0, so that the loads run under the MMAs
+      {
+        const i64 tn = t + gridDim.x;
+        if (tn < ntiles) {
+          const double2* src = psi + tile_base(tn, lane, my_rest) + toff;
+#pragma unroll
+          for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
+        }
+      }
       if (g == 0) {
         // the MMAs overwrite TMEM: wait until the epilogue has read tile it - 1
         bool ok = it == 0 || mbar_wait(mtfree, (uint32_t)(it - 1) & 1);
@@ -505,13 +527,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           abort_flag = 1;
         }
       }
-      // prefetch the next tile into registers while the MMAs run
-      const i64 tn = t + gridDim.x;
-      if (tn < ntiles) {
-        const double2* src = psi + tile_base(tn, lane, my_rest) + toff;
-#pragma unroll
-        for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
-      }
     }
     // on an abort, give the last issued MMAs one more bounded wait so that
     // tensor memory is not freed under them
@@ -522,8 +537,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const int erow = 32 * (ew & 3) + lane;
     const int ehalf = ew >> 2;
     const uint32_t trow = tmem + ((uint32_t)(32 * (ew & 3)) << 16);
-    const uint32_t srd = geo.sread_lo[g];
-    double2* stage = (double2*)(sm + OZ_OFF_STAGE);
+    const i64 myrow = geo.rowoff[erow];
     int it = 0;
     for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
       if (g == 0) {
@@ -535,9 +549,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       oz_bar(2);
       if (e_stop) break;
       const int scale = tile_scale[it & 1];
+      double2* dst = psi + tile_base(t, lane, my_rest) + myrow;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       // combine the seven levels of 8 reals (4 amplitudes) at a time
-#pragma unroll 1
+#pragma unroll
       for (int q = 0; q < 4; ++q) {
         float acc[OZ_NLEVEL][8];
 #pragma unroll
@@ -553,22 +568,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             aim[l] = acc[l][e + 1];
           }
           if (FIX) {
-            const int k = scale + G.fexp[c] - 1029;
-            stage[erow ^ geo.scol[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
-                                                     oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
+            const OzShift k = oz_shift(scale + G.fexp[c] - 1029);
+            dst[geo.coloff[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
+                                              oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
           } else {
             const int sc = scale + G.fexp[c] - 2098;
-            stage[erow ^ geo.scol[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+            dst[geo.coloff[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
           }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       oz_bar(2);
       if (g == 0) oz_arrive(mtfree);  // TMEM of this tile read: the next MMAs may start
-      // store the tile (overlaps the next tile's MMAs)
-      double2* dst = psi + tile_base(t, lane, my_rest) + toff;
-#pragma unroll
-      for (int r = 0; r < OZ_STEPS; ++r) dst[geo.ghi[r]] = stage[srd ^ geo.sread_hi[r]];
     }
   }
   __syncthreads();
@@ -589,9 +600,7 @@ namespace {
 // (row groups 144 B = 9 groups apart), column bits 2+ the K chunk; a K-chunk
 // stride rotating by rot = 4, 2, 1 bank groups for t5 = 3, 4, 5 then puts the
 // 32 lanes on 32 distinct banks (t5 <= 1 leaves fewer distinct words: 2 or 4
-// wavefronts).  The staging slots keep every quarter-warp of 16-byte
-// accesses on 8 distinct bank groups, for the row-wise writes and for the
-// tile-order reads.
+// wavefronts).
 void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]) {
   std::vector<int> sorted_t = tbits;
   std::sort(sorted_t.begin(), sorted_t.end());
@@ -610,15 +619,10 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
     if (g != grp.end()) rowbit[i] = (int)(g - grp.begin());
     else colbit[i] = cbit[std::find(tbits.begin(), tbits.end(), pos[i]) - tbits.begin()];
   }
-  int t5 = 0, t3 = 0;
-  for (int b : tbits) {
-    t5 += b < 5;
-    t3 += b < 3;
-  }
+  int t5 = 0;
+  for (int b : tbits) t5 += b < 5;
   const uint32_t rot = t5 == 3 ? 4 : t5 == 4 ? 2 : 1;
   geo->a_lbo = OZ_A_LBO0 + 16 * rot;
-  const int g3 = 3 - t3;
-  auto scol = [&](uint32_t c) { return (uint32_t)((c << 7) ^ ((c << g3) & 7u)); };
   auto aoff = [&](uint32_t row, uint32_t c) {
     return (c >> 2) * geo->a_lbo + (row >> 3) * OZ_A_SBO + (row & 7) * 16 + (c & 3) * 4;
   };
@@ -639,7 +643,6 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
     uint32_t row, col;
     split(v, 0, 8, &dep, &row, &col);
     geo->aoff_lo[v] = aoff(row, col);
-    geo->sread_lo[v] = (uint16_t)(row ^ scol(col));
   }
   geo->g7 = (i64)1 << pos[7];
   for (int r = 0; r < OZ_STEPS; ++r) {
@@ -648,9 +651,17 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
     split(r, 8, 4, &dep, &row, &col);
     geo->ghi[r] = dep;
     geo->aoff_hi[r] = aoff(row, col);
-    geo->sread_hi[r] = (uint16_t)(row ^ scol(col));
   }
-  for (int c = 0; c < 32; ++c) geo->scol[c] = (uint16_t)scol((uint32_t)c);
+  for (int r = 0; r < 128; ++r) {
+    geo->rowoff[r] = 0;
+    for (int b = 0; b < 7; ++b)
+      if ((r >> b) & 1) geo->rowoff[r] |= (i64)1 << grp[b];
+  }
+  for (int c = 0; c < 32; ++c) {
+    geo->coloff[c] = 0;
+    for (int jt = 0; jt < 5; ++jt)
+      if ((c >> cbit[jt]) & 1) geo->coloff[c] |= (i64)1 << tbits[jt];
+  }
   geo->nrest = 0;
   for (int b = 0; b < n; ++b)
     if (std::find(pos.begin(), pos.end(), b) == pos.end()) geo->rest[geo->nrest++] = b;

@@ -5,14 +5,13 @@
 // calls: tile scale, balanced digits into the bf16 A slices (decoded back
 // from their byte offsets), the stacked B slices, the level accumulators as
 // exact integer sums (checked below 2^24, hence exact in FP32), the
-// combination into doubles, the staging slots and the stores.  Compares with
+// combination into doubles and the stores (row and column offsets).  Compares with
 // the block applied in FP64 for n = 12..15 and random, lowest and highest
 // block placements, plus states with a wide dynamic range: every output must
 // be within 2^-41 of 2^(E + F) (E, F the exponents of its tile and gate-row
 // scales, the worst-case bound of the fixed-point rounding over K = 64), and
 // the largest error over a Gaussian state within 1e-13 of its largest output.
-// Also counts shared-memory wavefronts of the A writes (4-byte) and of the
-// staging writes and reads (16-byte).  Then replays chains of three unitary
+// Also counts shared-memory wavefronts of the A writes (4-byte).  Then replays chains of three unitary
 // blocks in the fixed-point state format (k_fused5_oz<true> between
 // oz_to_fix and oz_from_fix) against the FP64 product.
 // No kernel is launched.
@@ -49,7 +48,7 @@ static int wavefronts(const uint32_t* off, int width) {
 
 // One launch of k_fused5_oz<true> replayed on a fixed-point state (X holds
 // the re, im integers of each amplitude): tile shift from the OR of the
-// magnitudes, oz_digits_fix, exact level sums, oz_combine_fix, staging.
+// magnitudes, oz_digits_f, exact level sums, oz_combine_fix, direct stores.
 static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, int* exact_fails) {
   OzGeom* geo = new OzGeom();
   OzGate* G = new OzGate();
@@ -105,7 +104,6 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
           Ad[s][rc.first][2 * rc.second + 1] = dim[s];
         }
       }
-    std::vector<int64_t> stage(2 * OZ_TILE, 0);
     for (int row = 0; row < 128; ++row)
       for (int c = 0; c < 32; ++c)
         for (int part = 0; part < 2; ++part) {
@@ -117,15 +115,10 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
             if (std::llabs(sum) >= (1ll << 24)) (*exact_fails)++;
             acc[l] = (float)sum;
           }
-          stage[2 * ((uint32_t)row ^ geo->scol[c]) + part] = oz_combine_fix(acc, sh + G->fexp[c] - 1029);
+          // the epilogue's direct store of (row, c)
+          X[2 * (base + geo->rowoff[row] + geo->coloff[c]) + part] =
+              oz_combine_fix(acc, oz_shift(sh + G->fexp[c] - 1029));
         }
-    for (int r = 0; r < OZ_STEPS; ++r)
-      for (int tid = 0; tid < OZ_GROUP; ++tid) {
-        const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
-        const i64 gi = gidx(tid, r);
-        X[2 * gi] = stage[2 * si];
-        X[2 * gi + 1] = stage[2 * si + 1];
-      }
   }
   delete geo;
   delete G;
@@ -326,8 +319,6 @@ int main() {
               if (wavefronts(off, 4) > (t5 >= 2 ? 1 : t5 == 1 ? 2 : 4)) bank_fails++;
             }
         }
-        std::vector<cd> stage(OZ_TILE, cd(1e300, 0));
-        std::vector<double> bstage(OZ_TILE, 0.0);
         for (int row = 0; row < 128; ++row)
           for (int c = 0; c < 32; ++c) {
             double vals[2];
@@ -343,35 +334,13 @@ int main() {
               }
               vals[part] = oz_combine(acc, exm + G->fexp[c] - 2098);
             }
-            const uint32_t si = (uint32_t)row ^ geo->scol[c];
-            if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
-            stage[si] = cd(vals[0], vals[1]);
-            bstage[si] = std::ldexp(1.0, (exm - 1022) + (G->fexp[c] - 1022) - 41);
-          }
-        if (t == 0)
-          for (int w = 0; w < 4; ++w)
-            for (int c = 0; c < 32; ++c) {
-              uint32_t off[32];
-              for (int l = 0; l < 32; ++l) off[l] = 16 * ((uint32_t)(32 * w + l) ^ geo->scol[c]);
-              if (wavefronts(off, 16) > 4) bank_fails++;
-            }
-        for (int r = 0; r < OZ_STEPS; ++r) {
-          for (int tid = 0; tid < OZ_GROUP; ++tid) {
-            const i64 gi = base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
+            // the epilogue's direct store of (row, c)
+            const i64 gi = base + geo->rowoff[row] + geo->coloff[c];
             if (gi < 0 || gi >= N) { bad = true; continue; }
-            const uint32_t si = (uint32_t)geo->sread_lo[tid] ^ geo->sread_hi[r];
-            if (si >= (uint32_t)OZ_TILE) { bad = true; continue; }
             wrote[gi]++;
-            out[gi] = stage[si];
-            bound[gi] = bstage[si];
+            out[gi] = cd(vals[0], vals[1]);
+            bound[gi] = std::ldexp(1.0, (exm - 1022) + (G->fexp[c] - 1022) - 41);
           }
-          if (t == 0)
-            for (int w = 0; w < OZ_GROUP / 32; ++w) {
-              uint32_t off[32];
-              for (int l = 0; l < 32; ++l) off[l] = 16 * ((uint32_t)geo->sread_lo[32 * w + l] ^ geo->sread_hi[r]);
-              if (wavefronts(off, 16) > 4) bank_fails++;
-            }
-        }
       }
       double err = 0, nrm = 0;
       int over = 0;
