@@ -219,8 +219,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     """complex64 legs of the brickwork circuit against complex128.
 
     ``passes``: the unfused gate list in shared-memory passes.  ``fused_tc``:
-    ``circ.fuse(5)``, whose uncontrolled 5-qubit blocks run on the tensor
-    cores (3xTF32) and the rest in passes; ``runs`` device-timed circuits give
+    the gate list fused by the engine (QGB_PLAN_FUSE), whose uncontrolled
+    5-qubit blocks run on the tensor cores (3xTF32) and the rest in passes; ``runs`` device-timed circuits give
     p50/p99.  Both results are renormalised in FP64 and compared with the
     complex128 blocked result (infidelity 1 - |<psi128|psi64>|^2).
     ``c128_per_gate_ms`` is one run of the plain complex128 per-gate path
@@ -233,8 +233,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     b64 = GB300Backend("complex64")
     st64 = DeviceState(n, "complex64")
     out = DeviceArray((2,), np.float64, rt)
-    fdescs = [describe_gate(g, b64) for g in circ.fuse(5).queue]
-    n5 = sum(1 for d in fdescs if len(d[0]) == 5 and not d[1])
+    fdescs = [describe_gate(g, b64) for g in circ.fuse(5).queue]  # for one representative 5-qubit block
+    nfused, n5 = b64.engine_gb.fuse_stats(descs, n if n >= 12 else 0)  # the engine's fusion of the gate list
 
     def infidelity():
         check(lib.qgb_inner_mixed(state.ptr, state.code, st64.ptr, st64.code, n, out.ptr,
@@ -242,12 +242,12 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
         re, im = out.to_numpy()
         return 1.0 - (re * re + im * im)
 
-    def timed(dl, reps):
+    def timed(dl, reps, fuse=False):
         ms = []
         for _ in range(reps):
             check(lib.qgb_state_zero(st64.ptr, n, st64.code, rt.stream))
             ev.start(rt.stream)
-            b64.engine_gb.apply_many(st64, dl, blocked=True)
+            b64.engine_gb.apply_many(st64, dl, blocked=True, fuse=fuse)
             ms.append(ev.stop_ms(rt.stream))
         return ms
 
@@ -260,8 +260,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     ms_p = timed(descs, 1)[0]
     norm_p = b64.engine_gb.renormalize(st64)  # FP64 renormalisation of the complex64 result
     inf_p = infidelity()
-    timed(fdescs, 2)
-    ms_f = sorted(timed(fdescs, runs))
+    timed(descs, 2, fuse=True)
+    ms_f = sorted(timed(descs, runs, fuse=True))
     norm_f = b64.engine_gb.renormalize(st64)
     inf_f = infidelity()
     # the tensor-core kernel alone: 10 launches of the first 5-qubit block
@@ -291,7 +291,7 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     # per-gate result: 1 - |<psi_per_gate|psi_fused>|^2 in FP64
     st2 = DeviceState(n, "complex128")
     check(lib.qgb_state_zero(st2.ptr, n, st2.code, rt.stream))
-    eng.apply_many(st2, fdescs, blocked=True)
+    eng.apply_many(st2, descs, blocked=True, fuse=True)
     check(lib.qgb_inner(state.ptr, st2.ptr, n, state.code, out.ptr, rt.scratch(lib.qgb_inner_scratch_bytes()),
                         rt.stream))
     re2, im2 = out.to_numpy()
@@ -302,7 +302,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     p99 = ms_f[min(len(ms_f) - 1, int(np.ceil(0.99 * len(ms_f))) - 1)]
     return {"passes": {"gate_ms": ms_p, "value": g64 / (ms_p * 1e-3) / 1e9, "unit": "GB/s",
                        "infidelity_vs_c128": inf_p, "norm_before_renormalisation": norm_p},
-            "fused_tc": {"blocks": len(fdescs), "tc_blocks_5q": n5, "runs": runs, "p50_ms": p50, "p99_ms": p99,
+            "fused_tc": {"fusion": "engine (QGB_PLAN_FUSE)", "fused_ops": nfused, "tc_blocks_5q": n5, "runs": runs,
+                         "p50_ms": p50, "p99_ms": p99,
                          "circuits_per_s": 1e3 / p50, "infidelity_vs_c128": inf_f,
                          "norm_before_renormalisation": norm_f, "tc_wait_timeouts": tc_timeout.value,
                          "k_fused5_tc_gbs": tc_gbs, "k_fused5_tc_bytes_per_launch": 2 * 2**n * 8,
@@ -335,13 +336,15 @@ def run_brickwork(args):
     gates = brickwork_gates(n, DEPTH, SEED)
     circ = Circuit(n)
     circ.add(gates)
-    mode = args.mode if args.mode != "auto" else ("fused" if n >= 12 else "blocked")
+    mode = args.mode if args.mode != "auto" else ("engine" if n >= 12 else "blocked")
     t0 = time.perf_counter()
     run_circ = circ.fuse(5) if mode == "fused" else circ
     fuse_s = time.perf_counter() - t0
     descs = [describe_gate(g, backend) for g in run_circ.queue]
     udescs = descs if run_circ is circ else [describe_gate(g, backend) for g in circ.queue]
-    backend.blocked = mode in ("blocked", "fused")
+    backend.blocked = mode in ("blocked", "fused", "engine")
+    backend.fuse = mode == "engine"
+    efuse = mode == "engine"
     ndense = sum(1 for g in gates if type(g).__name__ == "U3")
     ncz = len(gates) - ndense
     gbytes, mbytes = algorithmic_bytes(n, ndense, ncz, S)
@@ -357,6 +360,9 @@ def run_brickwork(args):
         else:
             seg.append(d)
     npasses += n_tc
+    if efuse:  # the engine's own fusion: its 5-qubit blocks and other ops
+        nfused, n_tc = eng.fuse_stats(descs, n if n >= 12 else 0)
+        npasses = nfused
     pass_bytes = (npasses * 2 * 2**n * S) if backend.blocked else gbytes
     state = DeviceState(n, dtype)
     allq = list(range(n))
@@ -364,7 +370,7 @@ def run_brickwork(args):
 
     def device_step(seed):
         check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
-        eng.apply_many(state, descs, blocked=backend.blocked)
+        eng.apply_many(state, descs, blocked=backend.blocked, fuse=efuse)
         probs = eng.probabilities(state, allq)
         check(lib.qgb_sample(probs.ptr, n, NSHOTS, seed, samp.ptr, None, rt.scratch(lib.qgb_sample_scratch_bytes(n)),
                              rt.stream))
@@ -399,7 +405,7 @@ def run_brickwork(args):
     # the gate passes of one circuit, CUDA events on the launch stream
     check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
     ev.start(rt.stream)
-    eng.apply_many(state, descs, blocked=backend.blocked)
+    eng.apply_many(state, descs, blocked=backend.blocked, fuse=efuse)
     gate_ms = ev.stop_ms(rt.stream)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -409,7 +415,9 @@ def run_brickwork(args):
         # circuit's first block, CUDA events on the launch stream
         from qibo_gb300 import _lib
 
-        blk = next(d for d, tc in zip(descs, is_tc) if tc)
+        # a representative 5-qubit block of the circuit (the Python packer's
+        # first one; the kernel's cost does not depend on which)
+        blk = next(d for d in (describe_gate(g, backend) for g in circ.fuse(5).queue) if len(d[0]) == 5 and not d[1])
         qs = _lib.int_array(blk[0])
         mat = np.ascontiguousarray(np.asarray(blk[2], dtype=np.complex128)).view(np.float64).ravel()
         mp = mat.ctypes.data_as(_lib.dp)
@@ -470,7 +478,9 @@ def run_brickwork(args):
             "config": {"workload": f"random U3+CZ brickwork n={n} depth {DEPTH} seed {SEED} + {NSHOTS} shots",
                        "mode": mode, "gates": len(gates), "state_passes": npasses, "tensor_core_blocks": n_tc,
                        "fusion": ("qibo Circuit.fuse(max_qubits=5), once before timing "
-                                  f"({fuse_s:.2f} s, {len(descs)} blocks)") if mode == "fused" else "none",
+                                  f"({fuse_s:.2f} s, {len(descs)} blocks)") if mode == "fused" else
+                                 (f"engine (QGB_PLAN_FUSE, inside every qgb_apply_circuit call): {len(descs)} gates -> "
+                                  f"{npasses} ops, {n_tc} 5-qubit blocks") if efuse else "none",
                        "arithmetic": (("5-qubit blocks: Ozaki scheme on BF16 tensor cores (47-bit fixed point, "
                                        "exact level sums, IEEE doubles out); " if n_tc and S == 16 else "")
                                       + ("double-float (FP32 pipe) in passes, IEEE FP64 reductions"
@@ -689,7 +699,7 @@ def main():
                     choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
-    ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the complex64 leg")
     ap.add_argument("--serving-requests", type=int, default=240)

@@ -118,8 +118,16 @@ typedef struct qgb_op {
 #define QGB_PLAN_BLOCKED 1
 #define QGB_PLAN_STRICT_FP64 2
 #define QGB_PLAN_NO_TC 8       /* fused 5-qubit blocks in shared-memory passes instead of on the tensor cores */
+#define QGB_PLAN_FUSE 16       /* with QGB_PLAN_BLOCKED: fuse the gate list into blocks of <= 5 qubits first
+                                  (greedy forward scan, Circuit.fuse's role, models/circuit.py:954-1003) */
 int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, int flags, void* stream);
+/* What QGB_PLAN_FUSE makes of a gate list (host only): the number of ops
+ * after fusion and how many of them are uncontrolled 5-qubit blocks (the
+ * ones the tensor cores take).  pad_nqubits: the state's qubit count when
+ * qgb_apply_circuit widens every block to 5 qubits (tensor cores in use and
+ * nqubits >= 12), else 0. */
+int qgb_fuse_stats(const qgb_op* ops, int nops, const double* coefs, int pad_nqubits, int* nops_out, int* nblocks5);
 /* Number of state passes QGB_PLAN_BLOCKED would launch for this gate list
  * (host only, no device work). */
 int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int nops, const double* coefs, int* npasses);

@@ -17,6 +17,7 @@ QGB_C64, QGB_C128 = 0, 1
 QGB_PLAN_BLOCKED = 1
 QGB_PLAN_STRICT_FP64 = 2
 QGB_PLAN_NO_TC = 8
+QGB_PLAN_FUSE = 16
 
 vp, i32, i64, u32, u64, f64, sz = C.c_void_p, C.c_int, C.c_int64, C.c_uint32, C.c_uint64, C.c_double, C.c_size_t
 ip = C.POINTER(C.c_int)
@@ -73,6 +74,7 @@ SIGNATURES = {
     "qgb_apply_swap": (i32, [vp, i32, i32, i32, i32, ip, i32, vp]),
     "qgb_apply_circuit": (i32, [vp, i32, i32, C.POINTER(QgbOp), i32, dp, i32, vp]),
     "qgb_plan_passes": (i32, [i32, i32, C.POINTER(QgbOp), i32, dp, ip]),
+    "qgb_fuse_stats": (i32, [C.POINTER(QgbOp), i32, dp, i32, ip, ip]),
     "qgb_apply_fused5_tc": (i32, [vp, i32, i32, ip, dp, vp]),
     "qgb_tc_status": (i32, [ip]),
     "qgb_probs_scratch_bytes": (sz, [i32, i32]),

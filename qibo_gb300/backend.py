@@ -58,6 +58,10 @@ def describe_gate(gate, backend):
     return tuple(gate.qubits), (), m
 
 
+# below this size the tensor-core block kernels do not run and dense 5-qubit
+# blocks would only slow the shared-memory passes
+FUSE_MIN_QUBITS = 12
+
 class GB300Methods:
     """Hot-path overrides; expects ``self.dtype`` and the result classes."""
 
@@ -79,6 +83,10 @@ class GB300Methods:
         # complex64 results renormalised with an FP64 norm after the circuit
         # (QIBO_GB300_RENORMALIZE=0 turns it off)
         self.renormalize_c64 = os.environ.get("QIBO_GB300_RENORMALIZE", "1") != "0"
+        # the engine fuses circuits of FUSE_MIN_QUBITS or more into blocks of
+        # <= 5 qubits whose 5-qubit blocks run on the tensor cores
+        # (QIBO_GB300_FUSE=0 turns it off)
+        self.fuse = os.environ.get("QIBO_GB300_FUSE", "1") != "0"
 
     # -- states -----------------------------------------------------------
     def zero_state(self, nqubits, density_matrix=False, dtype=None):
@@ -147,7 +155,8 @@ class GB300Methods:
                     dt = arr.dtype if arr.dtype in (np.complex64, np.complex128) else self.dtype
                     state = DeviceState.from_numpy(arr, dt)
             descs = [d for d in (describe_gate(g, self) for g in circuit.queue) if d is not None]
-            self.engine_gb.apply_many(state, descs, blocked=self.blocked, strict_fp64=self.strict_fp64)
+            self.engine_gb.apply_many(state, descs, blocked=self.blocked, strict_fp64=self.strict_fp64,
+                                      fuse=self.fuse and nqubits >= FUSE_MIN_QUBITS)
             if state.dtype == np.complex64 and self.renormalize_c64 and descs:
                 self.engine_gb.renormalize(state)
         except DeviceOutOfMemory:

@@ -545,6 +545,25 @@ extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_
   int st = check_state_args(state, dtype, "qgb_apply_circuit");
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  if ((flags & QGB_PLAN_BLOCKED) && (flags & QGB_PLAN_FUSE) && nops > 1) {
+    for (int i = 0; i < nops; ++i) {  // validate every gate before fusion absorbs it
+      GateOp g;
+      st = qgb_classify(nqubits, ops[i].qubits, ops[i].k, ops[i].controls, ops[i].ncontrols,
+                        coefs + ops[i].coef_offset, &g, "qgb_apply_circuit");
+      if (st) return st;
+    }
+    std::vector<qgb_op> fops;
+    std::vector<double> fcoefs;
+    // where the tensor cores take 5-qubit blocks, every block is widened to
+    // 5 qubits: one tensor-core pass beats a shared-memory pass with a dense
+    // 3-4 qubit block (complex128 double-float is FP32-pipe-bound), and the
+    // complex128 fixed-point chain stays unbroken
+    const bool tc = (flags & QGB_PLAN_NO_TC) == 0 &&
+                    (dtype == QGB_C64 || (dtype == QGB_C128 && nqubits >= 12 && !(flags & QGB_PLAN_STRICT_FP64)));
+    qgb_fuse5(ops, nops, coefs, &fops, &fcoefs, tc && nqubits >= 12 ? nqubits : 0);
+    return qgb_run_blocked(state, nqubits, dtype, fops.data(), (int)fops.size(), fcoefs.data(),
+                           (flags & QGB_PLAN_STRICT_FP64) != 0, (flags & QGB_PLAN_NO_TC) == 0, s);
+  }
   if (flags & QGB_PLAN_BLOCKED)
     return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0,
                            (flags & QGB_PLAN_NO_TC) == 0, s);

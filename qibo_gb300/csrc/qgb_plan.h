@@ -39,3 +39,9 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
 bool qgb_oz_unitary(const GateOp& g);
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);
 int qgb_tc_prepare();  // allocate the tensor-core paths' device buffers (idempotent)
+
+// Engine-side fusion into blocks of at most 5 qubits (qgb_fuse.cu).
+// pad_nqubits >= 5: widen every block to 5 qubits (identity on the lowest
+// qubits of the pad_nqubits-qubit state it lacks); 0: no padding.
+void qgb_fuse5(const qgb_op* ops, int nops, const double* coefs, std::vector<qgb_op>* ops_out,
+               std::vector<double>* coefs_out, int pad_nqubits);

@@ -17,8 +17,9 @@
 // One thread issues
 //   D = A_hi*B_hi + A_hi*B_lo + A_lo*B_hi     (3xTF32, FP32 accumulation)
 // as 24 tcgen05.mma.kind::tf32 instructions (M=128, N=64, K=8) into tensor
-// memory, commits them to an mbarrier and waits on it; meanwhile the other
-// threads load the next tile into registers and park at the CTA barrier.
+// memory, commits them to an mbarrier and waits on it; all threads have
+// issued the loads of the next tile into registers just before, and the
+// others park at the CTA barrier.
 // Warps w and w+4 then read TMEM lanes 32(w%4).. (the groups) in two column
 // halves with tcgen05.ld, stage the outputs in shared memory in tile order,
 // and the CTA stores the tile back with the coalesced pattern of the load.
@@ -191,6 +192,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
+    // prefetch the next tile into registers while the MMAs run; issued
+    // before the MMAs, whose issue blocks thread 0 and with it warp 0
+    const i64 tn = t + gridDim.x;
+    i64 nbase = 0;
+    if (tn < ntiles) {
+      nbase = tile_base(tn, lane, my_rest);
+      const float2* src = psi + nbase + toff;
+#pragma unroll
+      for (int r = 0; r < TC_STEPS; ++r)
+        if (FULL || (tval && r < nr)) v[r] = src[geo.ghi[r]];
+    }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       uint32_t acc = 0;
@@ -213,16 +225,6 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
                    : "memory");
-    }
-    // prefetch the next tile into registers while the MMAs run
-    const i64 tn = t + gridDim.x;
-    i64 nbase = 0;
-    if (tn < ntiles) {
-      nbase = tile_base(tn, lane, my_rest);
-      const float2* src = psi + nbase + toff;
-#pragma unroll
-      for (int r = 0; r < TC_STEPS; ++r)
-        if (FULL || (tval && r < nr)) v[r] = src[geo.ghi[r]];
     }
     // one thread waits for the MMAs; the rest park at the barrier
     if (tid == 0 && !mbar_wait(mb, phase)) abort_flag = 1;

@@ -43,19 +43,36 @@ class Engine:
                                       m.ctypes.data_as(_lib.dp), self.rt.stream))
 
     def apply_many(self, state: DeviceState, descs: Iterable[GateDesc], blocked: bool = False,
-                   strict_fp64: bool = False):
+                   strict_fp64: bool = False, fuse: bool = False):
         """Apply a gate list with one C call (``qgb_apply_circuit``).
 
         ``blocked`` plans shared-memory passes (many gates per read+write of
         the state); complex128 passes then compute in double-float unless
-        ``strict_fp64``."""
+        ``strict_fp64``.  ``fuse`` (with ``blocked``) first fuses the list into
+        blocks of at most 5 qubits, whose uncontrolled 5-qubit blocks run on
+        the tensor cores."""
         descs = list(descs)
         if not descs:
             return
         ops, allc = self.pack_ops(descs)
         flags = (_lib.QGB_PLAN_BLOCKED if blocked else 0) | (_lib.QGB_PLAN_STRICT_FP64 if strict_fp64 else 0)
+        if blocked and fuse:
+            flags |= _lib.QGB_PLAN_FUSE
         check(self.lib.qgb_apply_circuit(state.ptr, state.nqubits, state.code, ops, len(descs),
                                          allc.ctypes.data_as(_lib.dp), flags, self.rt.stream))
+
+    def fuse_stats(self, descs: Iterable[GateDesc], pad_nqubits: int = 0):
+        """(ops after engine fusion, uncontrolled 5-qubit blocks among them);
+        ``pad_nqubits``: the state's size when the engine widens blocks to 5
+        qubits (tensor cores in use, 12 qubits or more)."""
+        descs = list(descs)
+        if not descs:
+            return 0, 0
+        ops, allc = self.pack_ops(descs)
+        a, b = C.c_int(0), C.c_int(0)
+        check(self.lib.qgb_fuse_stats(ops, len(descs), allc.ctypes.data_as(_lib.dp), pad_nqubits, C.byref(a),
+                                      C.byref(b)))
+        return a.value, b.value
 
     def count_passes(self, nqubits: int, dtype_code: int, descs: Iterable[GateDesc]) -> int:
         """State passes the shared-memory planner makes for this gate list."""

@@ -49,11 +49,12 @@ def make_circuit(n, ops):
     return c
 
 
-def run(backend, n, ops, psi=None, dtype="complex128", blocked=None, strict=False):
+def run(backend, n, ops, psi=None, dtype="complex128", blocked=None, strict=False, fuse=True):
     backend.set_dtype(dtype)
     if blocked is not None:
         backend.blocked = blocked
     backend.strict_fp64 = strict
+    backend.fuse = fuse
     try:
         res = backend.execute_circuit(make_circuit(n, ops), None if psi is None else psi.copy())
         return np.asarray(res.state())
@@ -61,6 +62,7 @@ def run(backend, n, ops, psi=None, dtype="complex128", blocked=None, strict=Fals
         backend.set_dtype("complex128")
         backend.blocked = True
         backend.strict_fp64 = False
+        backend.fuse = True
 
 
 def rand_state(n, seed, dtype=np.complex128):
@@ -131,12 +133,16 @@ def test_every_position_every_kind(backend, n):
 
 @pytest.mark.parametrize("n", [16, 20])
 def test_deep_random_circuit_c128_passes(backend, n):
-    """890-gate-scale accuracy of the double-float passes: a depth-30 U3+CZ
-    brickwork plus QFT against the FP64 oracle."""
+    """890-gate-scale accuracy of the double-float passes (engine fusion off)
+    and of the default engine-fused path: a depth-30 U3+CZ brickwork plus
+    QFT against the FP64 oracle."""
     ops = ref.brickwork_ops(n, 30, 5) + ref.qft_ops(n)
     psi = rand_state(n, 77)
     want = ref.execute(ops, n, psi)
-    got = run(backend, n, ops, psi, blocked=True)
+    got = run(backend, n, ops, psi, blocked=True, fuse=False)
+    assert np.max(np.abs(got - want)) < TOL128
+    # the default: engine fusion, 5-qubit blocks on the tensor cores
+    got = run(backend, n, ops, psi, blocked=True, fuse=True)
     assert np.max(np.abs(got - want)) < TOL128
 
 

@@ -165,3 +165,27 @@ def test_oz_chain_unnormalised_state(scale_last):
     for q, u in blocks:
         want = ref.apply_gate(want, u, list(q), n)
     assert np.max(np.abs(got - want)) < 1e-12 * 7.3
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 2e-5)])
+def test_engine_fusion_matches_oracle(dtype, tol):
+    """The backend's default path for n >= 12: the engine fuses the gate
+    list (qgb_fuse5) and runs its 5-qubit blocks on the tensor cores; a
+    depth-20 brickwork plus QFT (controlled phases and swaps) against the
+    FP64 oracle."""
+    from qibo_gb300 import Circuit, gates
+    from qibo_gb300.backend import GB300Backend, describe_gate
+
+    n = 16
+    ops = ref.brickwork_ops(n, 20, 8) + ref.qft_ops(n)
+    c = Circuit(n)
+    for nm, q, p in ops:
+        c.add(getattr(gates, nm)(*q, *p))
+    b = GB300Backend(dtype)
+    assert b.fuse
+    nops, n5 = b.engine_gb.fuse_stats([describe_gate(g, b) for g in c.queue])
+    assert n5 >= 20 and nops < len(ops) // 5
+    psi = _rand_state(n, 3)
+    got = np.asarray(b.execute_circuit(c, psi.copy()).state())
+    want = ref.execute(ops, n, psi)
+    assert np.max(np.abs(got - want)) < tol

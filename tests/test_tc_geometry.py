@@ -1,4 +1,6 @@
-"""CPU checks of the tensor-core block kernels' host logic.
+"""CPU checks of the tensor-core block kernels' host logic and of the
+engine's gate fusion (``tests/native/fuse_check.cu``, includes
+``qgb_fuse.cu``).
 
 Compiles ``tests/native/tc_geometry_check.cu`` (complex64, includes
 ``qgb_tc.cu``) and ``tests/native/oz_check.cu`` (complex128 Ozaki scheme,
@@ -49,3 +51,10 @@ def test_tc_geometry_tables(tmp_path):
 def test_oz_complex128_blocks(tmp_path):
     out = _build_and_run(tmp_path, "oz_check")
     assert "index failures 0 exactness failures 0 bank-pattern failures 0" in out
+
+
+def test_engine_fusion(tmp_path):
+    """qgb_fuse5: random gate lists (dense, controlled, diagonal, wider than
+    5 qubits) fused vs gate by gate on CPU states, 1e-12."""
+    out = _build_and_run(tmp_path, "fuse_check")
+    assert "failures 0" in out
