@@ -184,35 +184,70 @@ class Events:
         return ms.value
 
 
-def serving_sample(nreq: int, rate: float, baseline_req: int):
-    """Bounded sample of the serving stream: ``nreq`` requests with Poisson
-    arrivals, qubits uniform in [10, 28], depth uniform in [5, 30], mixed
-    dtypes and outputs; plus the one-at-a-time complex128 per-gate path on
-    its first ``baseline_req`` requests (forced to complex128)."""
+def serving_sample(nreq: int, rates, baseline: bool = True):
+    """Bounded sample of the serving stream: ``nreq`` requests with qubits
+    uniform in [10, 28], depth uniform in [5, 30], mixed complex64/complex128
+    tags and outputs (state, 1e4 shots, Z-string expectation), served at each
+    Poisson arrival rate in ``rates`` (the same requests; only the arrival
+    times scale with the rate).  The highest rate is a burst: every request is
+    waiting at once, so circuits/s there is the server's throughput.  Then the
+    same requests tagged complex64 (engine fusion, 3xTF32 tensor-core blocks),
+    and the one-at-a-time complex128 per-gate path on the same requests
+    (tagged complex128) as the baseline; the infidelity of the complex64
+    states against the baseline's complex128 states is the largest over the
+    state outputs of <= 24 qubits."""
     from qibo_gb300.serving import Request, Server, make_stream
 
-    reqs = make_stream(nreq, rate, seed=2026)
+    def retag(reqs, dtype):
+        return [Request(r.rid, r.nqubits, dtype, r.ops, r.coefs, r.shape, r.output, r.nshots, r.zmask, r.seed,
+                        r.arrival) for r in reqs]
+
+    def keep_states(reqs):
+        return {r.rid: r.result for r in reqs if r.output == "state" and r.nqubits <= 24}
+
     srv = Server()
+    out = {"requests": nreq, "by_rate": []}
     try:
-        warm = make_stream(16, 0.0, seed=7, nmin=10, nmax=14, dmin=5, dmax=6)
-        srv.run(warm, realtime=False)
+        warm = make_stream(16, 0.0, seed=7, nmin=10, nmax=18, dmin=5, dmax=6)
+        srv.run(warm + retag(warm, "complex64"), realtime=False)
+        for rate in rates:
+            srv.stats.clear()
+            st = srv.run(make_stream(nreq, rate, seed=2026), realtime=True)
+            out["by_rate"].append({"arrival_rate_per_s": rate, "circuits_per_s": st["circuits_per_s"],
+                                   "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                                   "batched": st.get("batched_requests", 0), "fused": st.get("fused", 0),
+                                   "graph_replays": st.get("graph_replays", 0)})
+        c64 = retag(make_stream(nreq, max(rates), seed=2026), "complex64")
         srv.stats.clear()
-        st = srv.run(reqs, realtime=True)
+        st = srv.run(c64, realtime=True)
+        out["complex64_only"] = {"arrival_rate_per_s": max(rates), "circuits_per_s": st["circuits_per_s"],
+                                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"]}
+        c64_states = keep_states(c64)
+        del c64
     finally:
         srv.close()
-    base = [Request(r.rid, r.nqubits, "complex128", r.ops, r.coefs, r.shape, r.output, r.nshots, r.zmask, r.seed, 0.0)
-            for r in make_stream(baseline_req, 0.0, seed=2026)]
-    srv = Server(one_at_a_time=True)
-    try:
-        bst = srv.run(base, realtime=False)
-    finally:
-        srv.close()
-    return {"requests": nreq, "arrival_rate_per_s": rate, "circuits_per_s": st["circuits_per_s"],
-            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "batched": st.get("batched_requests", 0),
-            "graph_replays": st.get("graph_replays", 0),
-            "baseline_one_at_a_time_c128_per_gate": {"requests": baseline_req,
-                                                     "circuits_per_s": bst["circuits_per_s"],
-                                                     "p50_ms": bst["p50_ms"], "p99_ms": bst["p99_ms"]}}
+    best = max(out["by_rate"], key=lambda d: d["circuits_per_s"])
+    out.update({"circuits_per_s": best["circuits_per_s"], "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
+                "arrival_rate_per_s": best["arrival_rate_per_s"]})
+    if baseline:
+        base = retag(make_stream(nreq, max(rates), seed=2026), "complex128")  # same requests, all waiting
+        srv = Server(one_at_a_time=True)
+        try:
+            bst = srv.run(base, realtime=False)
+        finally:
+            srv.close()
+        inf = 0.0
+        for r in base:
+            if r.rid in c64_states:
+                a = r.result.astype(np.complex128)
+                b = c64_states[r.rid].astype(np.complex128)
+                inf = max(inf, 1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
+        out["baseline_one_at_a_time_c128_per_gate"] = {"requests": nreq, "circuits_per_s": bst["circuits_per_s"],
+                                                        "p50_ms": bst["p50_ms"], "p99_ms": bst["p99_ms"]}
+        out["speedup_vs_baseline"] = out["circuits_per_s"] / bst["circuits_per_s"]
+        out["complex64_only"]["speedup_vs_baseline"] = out["complex64_only"]["circuits_per_s"] / bst["circuits_per_s"]
+        out["complex64_only"]["max_infidelity_vs_c128"] = inf
+    return out
 
 
 def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8):
@@ -501,7 +536,7 @@ def run_brickwork(args):
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0 and world == 1 and args.serving_requests > 0:
         del state
-        line["serving"] = serving_sample(args.serving_requests, args.serving_rate, args.serving_baseline)
+        line["serving"] = serving_sample(args.serving_requests, args.serving_rates)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -562,7 +597,7 @@ def run_vqe24(args):
 
 def run_serving(args):
     print(json.dumps({"workload": "serving stream sample",
-                      **serving_sample(args.serving_requests or 2000, args.serving_rate, args.serving_baseline)}))
+                      **serving_sample(args.serving_requests, args.serving_rates)}))
 
 
 def run_tc5(args):
@@ -702,10 +737,11 @@ def main():
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the complex64 leg")
-    ap.add_argument("--serving-requests", type=int, default=240)
-    ap.add_argument("--serving-rate", type=float, default=12.0)
-    ap.add_argument("--serving-baseline", type=int, default=40)
+    ap.add_argument("--serving-requests", type=int, default=120)
+    ap.add_argument("--serving-rates", default="25,50,10000",
+                    help="comma-separated Poisson arrival rates (requests/s) of the serving sample")
     args = ap.parse_args()
+    args.serving_rates = [float(x) for x in args.serving_rates.split(",")]
     if args.impl == "reference":
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,

@@ -39,6 +39,8 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
 bool qgb_oz_unitary(const GateOp& g);
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);
 int qgb_tc_prepare();  // allocate the tensor-core paths' device buffers (idempotent)
+int qgb_oz_stream_prepare(cudaStream_t s);  // complex128 chain scratch of stream s (qgb_tc128.cu)
+int qgb_oz_stream_release(cudaStream_t s);  // and its release before the stream is destroyed
 
 // Engine-side fusion into blocks of at most 5 qubits (qgb_fuse.cu).
 // pad_nqubits >= 5: widen every block to 5 qubits (identity on the lowest

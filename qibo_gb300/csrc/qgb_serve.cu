@@ -20,11 +20,16 @@ extern "C" {
 int qgb_stream_create(void** stream) {
   if (!stream) { qgb_set_error("qgb_stream_create: null"); return QGB_ERR_INVALID; }
   QGB_TRY_CUDA(cudaStreamCreateWithFlags((cudaStream_t*)stream, cudaStreamNonBlocking));
-  return QGB_OK;
+  // the stream's own complex128 chain scratch, so that circuits run on it
+  // later allocate nothing and share nothing with other streams
+  return qgb_oz_stream_prepare((cudaStream_t)*stream);
 }
 
 int qgb_stream_destroy(void* stream) {
-  if (stream) QGB_TRY_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+  if (!stream) return QGB_OK;
+  int st = qgb_oz_stream_release((cudaStream_t)stream);
+  if (st) return st;
+  QGB_TRY_CUDA(cudaStreamDestroy((cudaStream_t)stream));
   return QGB_OK;
 }
 

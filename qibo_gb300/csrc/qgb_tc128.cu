@@ -50,6 +50,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <unordered_map>
 #include <vector>
 
 #include "qgb_plan.h"
@@ -765,9 +767,25 @@ extern "C" int qgb_norm2(const void* state, int nqubits, int dtype, double* out,
 extern "C" size_t qgb_norm_scratch_bytes(void);
 
 namespace {
-double* g_oz_norm = nullptr;  // chain scratch: ||psi||^2, the scale e, the norm reduction
-int* g_oz_e = nullptr;
-void* g_oz_scratch = nullptr;
+// Chain scratch: ||psi||^2, the scale e and the norm reduction.  One set per
+// stream, so that chains on different streams (the serving loop's slots) do
+// not share it; the set of the default stream (and of any stream first seen
+// while it is being captured) is made by qgb_tc_prepare.
+struct OzChainScratch {
+  double* norm = nullptr;
+  int* e = nullptr;
+  void* red = nullptr;
+};
+OzChainScratch g_oz_default;
+std::mutex g_oz_mu;
+std::unordered_map<cudaStream_t, OzChainScratch> g_oz_streams;
+
+int oz_scratch_alloc(OzChainScratch* c) {
+  QGB_TRY_CUDA(cudaMalloc(&c->norm, sizeof(double)));
+  QGB_TRY_CUDA(cudaMalloc(&c->e, sizeof(int)));
+  QGB_TRY_CUDA(cudaMalloc(&c->red, qgb_norm_scratch_bytes()));
+  return QGB_OK;
+}
 }  // namespace
 
 // Device buffers of the tensor-core paths (error flag, chain scratch),
@@ -775,11 +793,50 @@ void* g_oz_scratch = nullptr;
 // qgb_apply_circuit finds them in place.
 int qgb_tc_prepare() {
   if (!qgb_tc_err_flag()) return QGB_ERR_CUDA;
-  if (!g_oz_norm) {
-    QGB_TRY_CUDA(cudaMalloc(&g_oz_norm, sizeof(double)));
-    QGB_TRY_CUDA(cudaMalloc(&g_oz_e, sizeof(int)));
-    QGB_TRY_CUDA(cudaMalloc(&g_oz_scratch, qgb_norm_scratch_bytes()));
+  std::lock_guard<std::mutex> lk(g_oz_mu);
+  if (!g_oz_default.norm) return oz_scratch_alloc(&g_oz_default);
+  return QGB_OK;
+}
+
+// Chain scratch of stream s, allocated on its first use outside a capture
+// (qgb_stream_create calls this so that the serving loop never allocates).
+int qgb_oz_stream_scratch(cudaStream_t s, OzChainScratch** out) {
+  int st = qgb_tc_prepare();
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_oz_mu);
+  *out = &g_oz_default;
+  if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return QGB_OK;
+  auto it = g_oz_streams.find(s);
+  if (it != g_oz_streams.end()) {
+    *out = &it->second;
+    return QGB_OK;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  QGB_TRY_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return QGB_OK;
+  OzChainScratch c;
+  st = oz_scratch_alloc(&c);
+  if (st) return st;
+  *out = &(g_oz_streams[s] = c);
+  return QGB_OK;
+}
+
+int qgb_oz_stream_prepare(cudaStream_t s) {
+  OzChainScratch* c;
+  return qgb_oz_stream_scratch(s, &c);
+}
+
+// Frees the chain scratch of a stream about to be destroyed (after the
+// stream's work is done).
+int qgb_oz_stream_release(cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_oz_mu);
+  auto it = g_oz_streams.find(s);
+  if (it == g_oz_streams.end()) return QGB_OK;
+  QGB_TRY_CUDA(cudaStreamSynchronize(s));
+  cudaFree(it->second.norm);
+  cudaFree(it->second.e);
+  cudaFree(it->second.red);
+  g_oz_streams.erase(it);
   return QGB_OK;
 }
 
@@ -788,21 +845,22 @@ int qgb_tc_prepare() {
 // the device), every block runs on it, and it is converted back.  Two extra
 // state passes replace the double <-> digit conversions of every block.
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s) {
-  int st = qgb_tc_prepare();
+  OzChainScratch* cs;
+  int st = qgb_oz_stream_scratch(s, &cs);
   if (st) return st;
-  st = qgb_norm2(state, n, QGB_C128, g_oz_norm, g_oz_scratch, (void*)s);
+  st = qgb_norm2(state, n, QGB_C128, cs->norm, cs->red, (void*)s);
   if (st) return st;
-  k_oz_scale<<<1, 1, 0, s>>>(g_oz_norm, g_oz_e);
+  k_oz_scale<<<1, 1, 0, s>>>(cs->norm, cs->e);
   QGB_LAUNCH_CHECK("k_oz_scale");
   const i64 N = (i64)1 << n;
   const int grid = (int)std::min<i64>((N + 255) / 256, (i64)qgb_num_sms() * 8);
-  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, g_oz_e);
+  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, cs->e);
   QGB_LAUNCH_CHECK("k_oz_to_fix");
   for (const GateOp* g : blocks) {
     st = qgb_launch_fused5_oz(state, n, *g, s, true);
     if (st) return st;
   }
-  k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, g_oz_e);
+  k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, cs->e);
   QGB_LAUNCH_CHECK("k_oz_from_fix");
   return QGB_OK;
 }

@@ -10,10 +10,14 @@ scheduler
 * runs small circuits (<= 13 qubits complex64, <= 12 complex128) many per
   launch through ``qgb_batch_run``, each CTA holding a whole state in shared
   memory and producing its output in the same kernel;
-* runs larger circuits as shared-memory passes on their own stream through
-  a ``qgb_program`` per circuit shape and slot, whose launches are captured
-  once as a CUDA graph and replayed with new matrices for later requests of
-  the same shape;
+* runs mid-sized circuits as shared-memory passes on their own stream
+  through a ``qgb_program`` per circuit shape and slot, whose launches are
+  captured once as a CUDA graph and replayed with new matrices for later
+  requests of the same shape;
+* runs circuits of ``fuse_min_qubits`` qubits or more, whose device time
+  dwarfs their launch overhead, through ``qgb_apply_circuit`` with engine
+  fusion: blocks of five qubits on the tensor cores (complex64 3xTF32,
+  complex128 Ozaki scheme), each slot's stream with its own chain scratch;
 * polls completion events without blocking, so work from requests that
   arrived at different times overlaps on the device.
 
@@ -245,7 +249,7 @@ class _Flight:
 
 class Server:
     def __init__(self, budget_bytes: Optional[int] = None, nslots: int = 16, batch_max: int = 256,
-                 use_graphs: bool = True, one_at_a_time: bool = False):
+                 use_graphs: bool = True, one_at_a_time: bool = False, fuse_min_qubits: int = 16):
         self.rt = Runtime.get()
         self.lib = self.rt.lib
         free, total = self.rt.mem_info()
@@ -255,6 +259,7 @@ class Server:
         self.nslots = 1 if one_at_a_time else nslots
         self.batch_max = batch_max
         self.use_graphs = use_graphs and not one_at_a_time
+        self.fuse_min_qubits = fuse_min_qubits
         self.streams, self.events, self.batch_ctx = [], [], []
         for _ in range(self.nslots):
             s, e, b = C.c_void_p(), C.c_void_p(), C.c_void_p()
@@ -336,6 +341,10 @@ class Server:
         if self.one_at_a_time:
             check(self.lib.qgb_apply_circuit(st, n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
                                              0, stream))
+        elif n >= self.fuse_min_qubits:
+            check(self.lib.qgb_apply_circuit(st, n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
+                                             _lib.QGB_PLAN_BLOCKED | _lib.QGB_PLAN_FUSE, stream))
+            self.stats["fused"] += 1
         else:
             key = (r.shape, r.dtype, slot)
             prog = self.programs.get(key)

@@ -170,3 +170,28 @@ def test_one_at_a_time_baseline_path():
     reqs = make_stream(6, rate=0.0, seed=9, nmin=10, nmax=14, dmin=3, dmax=5, nshots=500)
     stats = _serve(reqs, one_at_a_time=True)
     assert stats.get("batches", 0) == 0 and stats["large"] == 6
+
+
+def test_fused_large_requests_concurrent_vs_oracle():
+    """Requests of ``fuse_min_qubits`` qubits or more run through engine
+    fusion on the tensor cores, twelve slots at once (each stream with its
+    own complex128 fixed-point chain scratch); every state matches the FP64
+    oracle."""
+    from qibo_gb300.serving import Request, compile_brickwork
+
+    reqs, angs = [], {}
+    k = 0
+    for dtype in ("complex128", "complex64"):
+        for n in (16, 17, 18):
+            for d in (8, 10):
+                ang = np.random.default_rng(500 + k).uniform(0, 2 * np.pi, (d, n, 3))
+                ops, coefs = compile_brickwork(n, d, ang)
+                reqs.append(Request(k, n, dtype, ops, coefs, ("f", n, d), "state", 0, 0, 0))
+                angs[k] = (d, ang)
+                k += 1
+    stats = _serve(reqs, nslots=12)
+    assert stats.get("fused", 0) == len(reqs)
+    for r in reqs:
+        d, ang = angs[r.rid]
+        want = oracle_state(r.nqubits, d, ang, "complex128")
+        assert np.max(np.abs(r.result - want)) < TOL[r.dtype] * (10 if r.dtype == "complex64" else 1), (r.rid, r.dtype)
