@@ -585,6 +585,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
   }
   __syncthreads();
+  if (tid == 0 && abort_flag) atomicExch(err, 1);  // a wait gave up: reported by qgb_tc_status
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(OZ_TMEM_COLS));
 }
