@@ -198,6 +198,31 @@ int qgb_sample_noalloc(const double* probs, int m, int64_t nshots, uint64_t seed
 int qgb_philox_fill(uint32_t* out, int64_t n4, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                     void* stream);
 
+/* ---- measurement outcomes: expectation values from samples
+ *      (Backend.exp_value_diagonal_observable_symbolic_from_samples,
+ *      backends/abstract.py:2873-2926) and state collapse
+ *      (Backend.collapse_state / _collapse_statevector, :2424-2440,
+ *      :3279-3304) ---------------------------------------------------------- */
+/* odd[t] (device, int64) = number of samples[0..nshots) (device, int64
+ * outcome indices) whose bits under masks[t] have odd parity, for
+ * t < nterms (host masks).  Bit b of an outcome is bit b of the sampled
+ * index: for probabilities over qubits[0..m), qubit qubits[i] is bit m-1-i.
+ * Term t's mean of (-1)^parity over the shots is (nshots - 2 odd[t]) /
+ * nshots, the reference's frequency-weighted sum; integer counts make it
+ * independent of the reduction order. */
+#define QGB_PARITY_MAX_TERMS 256
+int qgb_parity_counts(const int64_t* samples, int64_t nshots, const uint64_t* masks, int nterms, int64_t* odd,
+                      void* stream);
+/* Collapse onto the outcome *outcome (device int64) of measuring qubits[0..nq)
+ * (qubits[0] is the most significant outcome bit, as in qgb_probabilities):
+ * amplitudes whose bits differ become 0; with ``normalize`` the kept ones are
+ * divided by the FP64 norm of the kept slice (a slice of norm 0 gives NaN,
+ * as in the reference).  The outcome is read on the device, so a shot drawn
+ * by qgb_sample collapses the state without a host round trip.  ``scratch``:
+ * qgb_norm_scratch_bytes() bytes (unused without ``normalize``). */
+int qgb_collapse(void* state, int nqubits, int dtype, const int* qubits, int nq, const int64_t* outcome,
+                 int normalize, void* scratch, void* stream);
+
 /* ---- expectation values: Backend.exp_value_observable_symbolic
  *      (backends/abstract.py:2946-3054) ------------------------------------ */
 /* out (device, float64) = sum_t coef[t] * <psi| P_t |psi> for Pauli strings

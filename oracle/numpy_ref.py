@@ -316,6 +316,92 @@ def samples_to_binary(samples: np.ndarray, nqubits: int) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
+# Collapse: backends/abstract.py:2424-2440, :3236-3247, :3279-3304
+# --------------------------------------------------------------------------
+
+def collapse_statevector(state: np.ndarray, qubits: Sequence[int], shot: int, nqubits: int,
+                         normalize: bool = True) -> np.ndarray:
+    """``Backend._collapse_statevector`` (:3279-3304) with ``_append_zeros``
+    (:3236-3247): transpose the measured qubits to the front, keep the slice
+    of outcome ``shot`` (qubits[0] the most significant bit), divide it by its
+    norm, and put the measured axes back with zeros on the other outcomes.
+    The axes go back in the order of ``qubits``, which is only the inverse
+    of the transpose for an ascending list (the reference's caller,
+    ``M.apply`` in gates/measurements.py:199-204, sorts them)."""
+    shape = state.shape
+    binshot = list(samples_to_binary(np.array([shot], dtype=np.int64), len(qubits))[0])
+    st = np.reshape(state, nqubits * (2,))
+    order = list(qubits) + [q for q in range(nqubits) if q not in qubits]
+    st = np.transpose(st, order)
+    subshape = (2 ** len(qubits),) + (nqubits - len(qubits)) * (2,)
+    st = np.reshape(st, subshape)[int(shot)]
+    if normalize:
+        st = st / np.sqrt(np.sum(np.abs(st) ** 2))
+    for q, r in zip(qubits, binshot):
+        st = np.expand_dims(st, q)
+        st = np.concatenate([np.zeros_like(st), st], axis=q) if r == 1 else np.concatenate([st, np.zeros_like(st)], axis=q)
+    return np.reshape(st, shape)
+
+
+# --------------------------------------------------------------------------
+# Expectation values from samples: backends/abstract.py:2873-2926, :3056-3140
+# --------------------------------------------------------------------------
+
+def exp_value_from_frequencies(frequencies: Dict[str, int], terms_qubits, terms_coefficients, qubit_map,
+                               constant: float = 0.0) -> float:
+    """``Backend.exp_value_diagonal_observable_symbolic_from_samples``
+    (:2873-2926) on a frequency table of bitstrings over ``qubit_map``: each
+    term is its coefficient times the frequency-weighted mean of
+    (-1)^(number of 1 bits on the term's qubits)."""
+    keys = list(frequencies.keys())
+    counts = np.array(list(frequencies.values()), dtype=np.float64)
+    counts = counts / counts.sum()
+    qubit_map = list(qubit_map)
+    expvals = []
+    for qubits, coefficient in zip(terms_qubits, terms_coefficients):
+        expvals.extend([coefficient * (-1) ** [k[qubit_map.index(q)] for q in qubits].count("1") for k in keys])
+    expvals = np.array(expvals, dtype=counts.dtype).reshape(len(terms_coefficients), len(frequencies))
+    return float(np.sum(expvals @ counts) + constant)
+
+
+def basis_rotation(factor: str):
+    """Matrix of ``basis_rotation()`` of the Pauli gate ``factor``
+    (gates/gates.py:191-292): X -> H, Y -> (Y + Z)/sqrt(2), Z -> none."""
+    if factor == "X":
+        return gate_matrix("H")
+    if factor == "Y":
+        return (gate_matrix("Y") + gate_matrix("Z")) / math.sqrt(2)
+    return None
+
+
+def exp_value_observable_symbolic_from_samples(state: np.ndarray, groups, nqubits: int, constant: float, nshots: int,
+                                               rng=None) -> float:
+    """``Backend.exp_value_observable_symbolic_from_samples`` (:3056-3140) on a
+    final state: for each group ``(coefficients, observables, qubits)`` the
+    state is rotated by the basis rotations of the group's measured qubits
+    (first non-identity factor per qubit), ``nshots`` outcomes of those
+    qubits are drawn, and their frequencies give the group's terms."""
+    total = 0.0
+    for coefs, observables, terms_qubits in groups:
+        measured = {}
+        for qubits, observable in zip(terms_qubits, observables):
+            for q, f in zip(qubits, observable):
+                if f != "I" and q not in measured:
+                    measured[q] = f
+        st = state
+        for q, f in measured.items():
+            m = basis_rotation(f)
+            if m is not None:
+                st = apply_gate(st, m.astype(state.dtype), (q,), nqubits)
+        qmap = list(measured)
+        probs = calculate_probabilities(st, qmap, nqubits)
+        freq = sample_frequencies(probs, nshots, rng)
+        bfreq = {f"{k:b}".zfill(len(qmap)): v for k, v in freq.items()}
+        total += exp_value_from_frequencies(bfreq, terms_qubits, coefs, qmap)
+    return total + constant
+
+
+# --------------------------------------------------------------------------
 # Expectation values: backends/abstract.py:2807-2825, :2946-3054
 # --------------------------------------------------------------------------
 

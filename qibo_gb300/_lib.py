@@ -45,6 +45,7 @@ QGB_NOT_READY = 6
 QGB_PROGRAM_NO_GRAPH = 4
 QGB_OUT_STATE, QGB_OUT_SAMPLES, QGB_OUT_ZEXP = 0, 1, 2
 QGB_BATCH_MAX_QUBITS = {0: 13, 1: 12}
+QGB_PARITY_MAX_TERMS = 256  # include/qgb300.h
 
 
 # name -> (restype, argtypes)
@@ -87,6 +88,8 @@ SIGNATURES = {
     "qgb_sample_noalloc": (i32, [vp, i32, i64, u64, vp, vp, vp]),
     "qgb_sample_state_scratch_bytes": (sz, [i32]),
     "qgb_sample_state": (i32, [vp, i32, i32, i64, u64, vp, vp, vp]),
+    "qgb_parity_counts": (i32, [vp, i64, u64p, i32, vp, vp]),
+    "qgb_collapse": (i32, [vp, i32, i32, ip, i32, vp, i32, vp, vp]),
     "qgb_expect_scratch_bytes": (sz, [i32, i32]),
     "qgb_expect_pauli": (i32, [vp, i32, i32, u64p, u64p, dp, i32, vp, vp, vp]),
     "qgb_expect_dense": (i32, [vp, i32, i32, vp, vp, vp, vp]),

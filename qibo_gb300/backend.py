@@ -16,6 +16,11 @@ reference method (abstract.py)     here
 ``sample_frequencies`` :2760       ``qgb_sample`` into a device histogram
 ``exp_value_observable_symbolic``  ``qgb_expect_pauli`` (one pass per flip
   :2946                            mask, all terms)
+``exp_value_observable_symbolic_``  basis rotations, device shots and
+  ``from_samples`` :3056           ``qgb_parity_counts`` per term group
+``collapse_state`` :2424           ``qgb_collapse`` (in place)
+``execute_circuit_repeated``       per shot on the device: collapsing
+  :2532                            measurements sampled and applied there
 ``set_seed`` :181                  seeds the Philox stream
 =================================  ==========================================
 
@@ -33,8 +38,9 @@ from typing import List
 
 import numpy as np
 
+from . import _lib
 from . import gates as G
-from ._lib import DeviceOutOfMemory
+from ._lib import DeviceOutOfMemory, check, int_array
 from .device import DeviceArray, DeviceState, Runtime
 from .engine import Engine, pauli_masks
 
@@ -134,7 +140,10 @@ class GB300Methods:
             raise NotImplementedError("qibo_gb300 simulates state vectors only")
         self._validate_nqubits(nqubits)
         if getattr(circuit, "repeated_execution", False):
-            raise NotImplementedError("collapse / noisy repeated execution is not supported by qibo_gb300")
+            if not circuit.measurements and not getattr(circuit, "has_collapse", False):
+                raise RuntimeError("Attempting to perform noisy simulation with `density_matrix=False` and no "
+                                   "Measurement gate in the Circuit.")
+            return self.execute_circuit_repeated(circuit, nshots, initial_state)
         if getattr(circuit, "accelerators", None):
             raise NotImplementedError("distributed (multi-GPU) circuits are not supported by qibo_gb300")
         if initial_state is not None and hasattr(initial_state, "queue") and hasattr(initial_state, "nqubits"):
@@ -176,6 +185,168 @@ class GB300Methods:
         if initial_states is None:
             initial_states = [None] * len(circuits)
         return [self.execute_circuit(c, s, nshots) for c, s in zip(circuits, initial_states)]
+
+    def execute_circuit_repeated(self, circuit, nshots, initial_state=None):
+        """Backend.execute_circuit_repeated (backends/abstract.py:2532-2636)
+        for circuits with collapsing measurements, on the device.  Every shot
+        runs the circuit again from the initial state.  A collapsing
+        measurement draws its outcome on the device from the FP64
+        probabilities of its sorted qubits (as gates/measurements.py:199-204),
+        and ``qgb_collapse`` projects the state onto it straight from device
+        memory.  The final measurements draw one shot each into a device
+        array.  The host only queues launches, and the outcomes come back
+        once, after the last shot."""
+        if getattr(circuit, "has_unitary_channel", False):
+            raise NotImplementedError("noisy repeated execution needs noise channels, not supported by qibo_gb300")
+        if getattr(circuit, "has_collapse", False) and not circuit.measurements:
+            raise RuntimeError("The circuit contains only collapsing measurements (`collapse=True`) but "
+                               "`density_matrix=False`. Please set `density_matrix=True` to retrieve the final "
+                               "state after execution.")
+        nqubits, nshots = circuit.nqubits, int(nshots)
+        eng, rt, lib = self.engine_gb, self.rt, self.rt.lib
+        flags = ((_lib.QGB_PLAN_BLOCKED if self.blocked else 0) | (_lib.QGB_PLAN_STRICT_FP64 if self.strict_fp64 else 0)
+                 | (_lib.QGB_PLAN_FUSE if self.blocked and self.fuse and nqubits >= FUSE_MIN_QUBITS else 0))
+        # the circuit as runs of gates (packed once) and collapsing measurements
+        items, run, collapse_gates = [], [], []
+        for g in circuit.queue:
+            if getattr(g, "symbolic_parameters", None):
+                raise NotImplementedError("parameters that depend on measurement outcomes are not supported")
+            if type(g).__name__ == "M":
+                if getattr(g, "collapse", False):
+                    if run:
+                        items.append(("gates", eng.pack_ops(run), len(run)))
+                        run = []
+                    qs = sorted(g.target_qubits)
+                    items.append(("collapse", int_array(qs), len(qs)))
+                    collapse_gates.append((g, len(qs)))
+                continue
+            d = describe_gate(g, self)
+            if d is not None:
+                run.append(d)
+        if run:
+            items.append(("gates", eng.pack_ops(run), len(run)))
+        meas_q = [q for m in circuit.measurements for q in m.target_qubits]
+        nmeas, ncol = len(meas_q), len(collapse_gates)
+        try:
+            state = DeviceState(nqubits, self.dtype)
+            init = None
+            if initial_state is not None:
+                init = self._as_device_state(initial_state)
+                if tuple(init.shape) != (2**nqubits,):
+                    raise ValueError(f"Given initial state has shape {tuple(init.shape)} instead of the expected "
+                                     f"{(2 ** nqubits,)}.")
+                if init.dtype != state.dtype:
+                    init = init.astype(state.dtype)
+            # device buffers for every shot, allocated once
+            col_probs = [DeviceArray((2**m,), np.float64, rt) for _, m in collapse_gates]
+            fin_probs = DeviceArray((2**nmeas,), np.float64, rt)
+            outcomes = DeviceArray((max(1, nshots * ncol),), np.int64, rt)
+            samples = DeviceArray((max(1, nshots),), np.int64, rt)
+            sizes = [lib.qgb_norm_scratch_bytes(), lib.qgb_sample_scratch_bytes(nmeas),
+                     lib.qgb_probs_scratch_bytes(nqubits, nmeas)]
+            sizes += [lib.qgb_sample_scratch_bytes(m) for _, m in collapse_gates]
+            sizes += [lib.qgb_probs_scratch_bytes(nqubits, m) for _, m in collapse_gates]
+            scratch = rt.scratch(max(sizes))
+            mq = int_array(meas_q)
+            code, s = state.code, rt.stream
+            for shot in range(nshots):
+                if init is None:
+                    check(lib.qgb_state_zero(state.ptr, nqubits, code, s))
+                else:
+                    check(lib.qgb_memcpy_d2d(state.ptr, init.ptr, state.nbytes, s))
+                j = 0
+                for kind, payload, k in items:
+                    if kind == "gates":
+                        ops, allc = payload
+                        check(lib.qgb_apply_circuit(state.ptr, nqubits, code, ops, k, allc.ctypes.data_as(_lib.dp),
+                                                    flags, s))
+                    else:
+                        out = outcomes.ptr + 8 * (shot * ncol + j)
+                        check(lib.qgb_probabilities(state.ptr, nqubits, code, payload, k, col_probs[j].ptr, scratch, s))
+                        check(lib.qgb_sample(col_probs[j].ptr, k, 1, self._next_key(), out, None, scratch, s))
+                        check(lib.qgb_collapse(state.ptr, nqubits, code, payload, k, out, 1, scratch, s))
+                        j += 1
+                check(lib.qgb_probabilities(state.ptr, nqubits, code, mq, nmeas, fin_probs.ptr, scratch, s))
+                check(lib.qgb_sample(fin_probs.ptr, nmeas, 1, self._next_key(), samples.ptr + 8 * shot, None,
+                                     scratch, s))
+            dec = samples.to_numpy()[:nshots]
+            col = outcomes.to_numpy()[: nshots * ncol].reshape(nshots, ncol) if ncol else None
+        except DeviceOutOfMemory:
+            raise RuntimeError(f"State does not fit in {self.device} memory.")
+        # each collapsing measurement keeps its outcomes, as gate.result.add_shot does
+        for j, (g, m) in enumerate(collapse_gates):
+            res = getattr(g, "result", None)
+            if res is not None and hasattr(res, "register_samples"):
+                res.register_samples(self.samples_to_binary(col[:, j], m))
+        binary = np.asarray(self.samples_to_binary(dec, nmeas))
+        result = self._outcomes_class()(circuit.measurements, backend=self, samples=binary, nshots=nshots)
+        if hasattr(result, "_repeated_execution_frequencies"):  # as backends/abstract.py:2631-2633
+            result._repeated_execution_frequencies = collections.Counter(
+                "".join(str(int(b)) for b in row) for row in binary)
+        circuit._final_state = result
+        return result
+
+    def collapse_state(self, state, qubits, shot, nqubits, normalize=True, density_matrix=False):
+        """Backend.collapse_state / _collapse_statevector
+        (backends/abstract.py:2424-2440, :3279-3304): keep the slice of the
+        state that agrees with outcome ``shot[0]`` of ``qubits`` (qubits[0]
+        the most significant bit), divided by its norm, zeros elsewhere.  On
+        the device and in place (qibojit's convention); returns the state."""
+        if density_matrix:
+            raise NotImplementedError("qibo_gb300 simulates state vectors only")
+        st = self._as_device_state(state)
+        outcome = int(np.asarray(shot).reshape(-1)[0])
+        self.engine_gb.collapse(st, list(qubits), outcome, normalize)
+        return st
+
+    def exp_value_observable_symbolic_from_samples(self, circuit, diagonal_terms_coefficients,
+                                                   diagonal_terms_observables, diagonal_terms_qubits, nqubits,
+                                                   constant, nshots):
+        """Backend.exp_value_observable_symbolic_from_samples
+        (backends/abstract.py:3056-3140) on the device.  The circuit runs
+        once.  For each group of terms measured together, a copy of the state
+        is rotated to the group's basis with the reference's basis rotations
+        (X: H, Y: (Y + Z)/sqrt(2), gates/gates.py:191-241).  ``nshots``
+        outcomes of the group's measured qubits are drawn on the device, and
+        each term's sample mean of (-1)^parity comes from integer parity
+        counts (qgb_parity_counts).  That is the reference's
+        frequency-weighted sum (:2873-2926) without moving the samples to
+        the host."""
+        saved = getattr(circuit, "_final_state", None)
+        try:
+            result = self.execute_circuit(circuit, nshots=nshots)
+            state = self._as_device_state(result.state())
+        finally:
+            circuit._final_state = saved
+        h = np.array([[1, 1], [1, -1]], dtype=np.complex128) / np.sqrt(2)
+        ybasis = np.array([[1, -1j], [1j, -1]], dtype=np.complex128) / np.sqrt(2)
+        expval = 0.0
+        for coefs, observables, terms_qubits in zip(diagonal_terms_coefficients, diagonal_terms_observables,
+                                                     diagonal_terms_qubits):
+            measured = {}
+            for qubits, observable in zip(terms_qubits, observables):
+                for q, factor in zip(qubits, observable):
+                    if factor != "I" and q not in measured:
+                        measured[q] = factor
+            qmap = list(measured)
+            masks = []
+            for qubits in terms_qubits:
+                mk = 0
+                for q in qubits:
+                    mk ^= 1 << (len(qmap) - 1 - qmap.index(q))
+                masks.append(mk)
+            if not qmap:
+                expval += sum(coefs)
+                continue
+            work = state.copy()
+            rot = [((q,), (), h if f == "X" else ybasis) for q, f in measured.items() if f in ("X", "Y")]
+            if rot:
+                self.engine_gb.apply_many(work, rot, blocked=self.blocked, strict_fp64=self.strict_fp64)
+            probs = self.engine_gb.probabilities(work, qmap)
+            samples = self.engine_gb.sample_device(probs, nshots, self._next_key())
+            means = self.engine_gb.parity_means(samples, nshots, masks)
+            expval += sum(c * m for c, m in zip(coefs, means))
+        return constant + expval
 
     # -- measurement --------------------------------------------------------
     def calculate_probabilities(self, state, qubits, nqubits, density_matrix=False):
@@ -307,3 +478,8 @@ class GB300Backend(GB300Methods, StandaloneBase):
         from .result import CircuitResult, QuantumState
 
         return QuantumState, CircuitResult
+
+    def _outcomes_class(self):
+        from .result import MeasurementOutcomes
+
+        return MeasurementOutcomes

@@ -27,7 +27,6 @@ class Circuit:
         self.accelerators = None
         self.queue = []
         self.measurements = []
-        self.repeated_execution = False
         self.has_collapse = False
         self.has_unitary_channel = False
         self._final_state = None
@@ -41,9 +40,31 @@ class Circuit:
         for q in gate.qubits:
             if q >= self.nqubits or q < 0:
                 raise ValueError(f"gate {gate} acts on qubit {q} of a {self.nqubits}-qubit circuit")
-        self.queue.append(gate)
         if isinstance(gate, G.M):
-            self.measurements.append(gate)
+            # basis rotations first, once (models/circuit.py:658-666)
+            for base in gate.basis:
+                if base not in self.queue:
+                    self.add(base)
+            self.queue.append(gate)
+            if gate.collapse:
+                self.has_collapse = True
+            else:
+                self.measurements.append(gate)
+            return gate.result
+        self.queue.append(gate)
+        # a gate after a measurement on the same qubits makes that measurement
+        # collapse the state (models/circuit.py:684-689)
+        for measurement in list(self.measurements):
+            if set(measurement.qubits) & set(gate.qubits):
+                measurement.collapse = True
+                self.has_collapse = True
+                self.measurements.remove(measurement)
+        return None
+
+    @property
+    def repeated_execution(self) -> bool:
+        """models/circuit.py:321-324 (no noise channels here)."""
+        return self.has_collapse or (self.has_unitary_channel and not self.density_matrix)
 
     @property
     def ngates(self):

@@ -157,6 +157,49 @@ class Engine:
                                       scratch, self.rt.stream))
         return out.to_numpy()
 
+    def sample_device(self, probs: DeviceArray, nshots: int, seed: int) -> DeviceArray:
+        """``nshots`` outcome indices drawn from device FP64 ``probs`` (length
+        2^m), left on the device (int64)."""
+        m = int(probs.shape[0]).bit_length() - 1
+        if 2**m != probs.shape[0]:
+            raise ValueError("probability vector length must be a power of two")
+        scratch = self.rt.scratch(self.lib.qgb_sample_scratch_bytes(m))
+        out = DeviceArray((max(1, int(nshots)),), np.int64, self.rt)
+        check(self.lib.qgb_sample(probs.ptr, m, int(nshots), int(seed) & (2**64 - 1), out.ptr, None, scratch,
+                                  self.rt.stream))
+        return out
+
+    def parity_means(self, samples: DeviceArray, nshots: int, masks: Sequence[int]) -> np.ndarray:
+        """Per mask, the mean over the shots of (-1)^(number of 1 bits of the
+        outcome under the mask), from integer parity counts on the device."""
+        masks = [int(m) for m in masks]
+        out = np.ones(len(masks), dtype=np.float64)
+        if nshots <= 0:
+            return out
+        for lo in range(0, len(masks), _lib.QGB_PARITY_MAX_TERMS):
+            chunk = masks[lo:lo + _lib.QGB_PARITY_MAX_TERMS]
+            odd = DeviceArray((len(chunk),), np.int64, self.rt)
+            mp = (C.c_uint64 * len(chunk))(*chunk)
+            check(self.lib.qgb_parity_counts(samples.ptr, int(nshots), mp, len(chunk), odd.ptr, self.rt.stream))
+            out[lo:lo + len(chunk)] = (nshots - 2 * odd.to_numpy()) / nshots
+        return out
+
+    def collapse(self, state: DeviceState, qubits: Sequence[int], outcome, normalize: bool = True):
+        """Project ``state`` in place onto ``outcome`` of measuring ``qubits``
+        (``qubits[0]`` the most significant outcome bit); ``outcome`` is an
+        int or a device int64 array whose first element is the outcome."""
+        qubits = list(qubits)
+        if not isinstance(outcome, DeviceArray):
+            k = int(outcome)
+            if not 0 <= k < 2 ** len(qubits):
+                raise ValueError(f"outcome {k} outside the {2 ** len(qubits)} outcomes of {len(qubits)} qubits")
+            dev = DeviceArray((1,), np.int64, self.rt)
+            self.rt.h2d(dev.ptr, np.array([k], dtype=np.int64))
+            outcome = dev
+        scratch = self.rt.scratch(self.lib.qgb_norm_scratch_bytes())
+        check(self.lib.qgb_collapse(state.ptr, state.nqubits, state.code, int_array(qubits), len(qubits),
+                                    outcome.ptr, int(bool(normalize)), scratch, self.rt.stream))
+
     def expect_pauli(self, state: DeviceState, xmask: Sequence[int], zmask: Sequence[int],
                      coef: Sequence[float]) -> float:
         """sum_t coef[t] <psi|P_t|psi>, P_t given by qubit bit masks (bit q = qubit q)."""

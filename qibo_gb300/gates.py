@@ -212,22 +212,77 @@ class Unitary(Gate):
         return self._matrix
 
 
+class MeasurementResult:
+    """Outcomes of one measurement gate (measurements.py:61-163): the samples
+    registered after execution, one binary row per shot."""
+
+    def __init__(self, gate):
+        self.gate = gate
+        self._samples = None
+
+    def register_samples(self, samples):
+        self._samples = np.asarray(samples)
+
+    def has_samples(self):
+        return self._samples is not None
+
+    def samples(self, binary: bool = True):
+        if self._samples is None:
+            raise RuntimeError("the measurement has no samples: execute the circuit first")
+        if binary:
+            return self._samples
+        n = self._samples.shape[-1]
+        return (self._samples @ (2 ** np.arange(n - 1, -1, -1))).astype(np.int64)
+
+    def reset(self):
+        self._samples = None
+
+
+def _basis_rotation(basis, q):
+    """The gate that rotates ``basis`` onto Z on qubit q (X: H, Y: (Y + Z)/sqrt(2),
+    Z: none; gates/gates.py:191-292)."""
+    name = basis if isinstance(basis, str) else getattr(basis, "__name__", str(basis))
+    if name == "Z":
+        return None
+    if name == "X":
+        return H(q)
+    if name == "Y":
+        return Unitary(np.array([[1, -1j], [1j, -1]], dtype=np.complex128) / np.sqrt(2), q)
+    raise NotImplementedError(f"measurement basis {name}: only X, Y and Z are supported")
+
+
 class M(Gate):
-    """Measurement of ``qubits`` (gates/measurements.py:11); a no-op on the
-    state unless ``collapse=True`` (not supported here)."""
+    """Measurement of ``qubits`` (gates/measurements.py:11-218).  A no-op on
+    the state, except that ``collapse=True`` measures during the circuit:
+    the state is projected onto the drawn outcome and the circuit runs once
+    per shot (the backend's ``execute_circuit_repeated``).  ``basis`` (X, Y
+    or Z, one for all qubits or one per qubit) adds the reference's basis
+    rotations before the measurement (gates/measurements.py:96-105)."""
 
     def __init__(self, *q, register_name=None, collapse: bool = False, basis=None, p0=None, p1=None):
         super().__init__(*q)
-        if collapse:
-            raise NotImplementedError("collapsing measurements are not supported by qibo_gb300")
+        if p0 is not None or p1 is not None:
+            raise NotImplementedError("bit-flip measurement noise is not supported by qibo_gb300")
         self.register_name = register_name
-        self.collapse = False
+        self.collapse = bool(collapse)
+        bases = basis if isinstance(basis, (list, tuple)) else [basis or "Z"] * len(self.target_qubits)
+        if len(bases) != len(self.target_qubits):
+            raise ValueError(f"Given basis list has length {len(bases)} while the measurement acts on "
+                             f"{len(self.target_qubits)} qubits.")
+        self.basis = [g for g in (_basis_rotation(b, q) for b, q in zip(bases, self.target_qubits)) if g is not None]
+        self.result = MeasurementResult(self)
 
     def matrix(self, backend=None):
         raise NotImplementedError("measurement gates have no matrix")
 
     def apply(self, backend, state, nqubits):
-        return state
+        if not self.collapse:
+            return state
+        qubits = sorted(self.target_qubits)
+        probs = backend.calculate_probabilities(state, qubits, nqubits)
+        shot = backend.sample_shots(probs, 1)
+        self.result.register_samples(backend.samples_to_binary(np.asarray(shot), len(qubits)))
+        return backend.collapse_state(state, qubits, shot, nqubits)
 
 
 class FusedGate(Gate):

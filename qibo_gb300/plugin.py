@@ -21,7 +21,7 @@ def qibo_backend_class():
     if _CLASS is not None:
         return _CLASS
     from qibo.backends.numpy import NumpyBackend
-    from qibo.result import CircuitResult, QuantumState
+    from qibo.result import CircuitResult, MeasurementOutcomes, QuantumState
 
     from .backend import GB300Methods
     from .device import DeviceArray
@@ -44,6 +44,9 @@ def qibo_backend_class():
 
         def _result_classes(self):
             return QuantumState, CircuitResult
+
+        def _outcomes_class(self):
+            return MeasurementOutcomes
 
     _CLASS = QiboGB300Backend
     return _CLASS

@@ -107,3 +107,44 @@ class CircuitResult(QuantumState):
             return self._samples
         n = len(self.measured_qubits)
         return (np.asarray(self._samples) @ (2 ** np.arange(n - 1, -1, -1))).astype(np.int64)
+
+
+class MeasurementOutcomes(CircuitResult):
+    """Measurement outcomes without a final state (result.py:166-548): what
+    repeated execution returns, with one sample per shot.  Probabilities are
+    the observed frequencies over the shots (result.py:211-230)."""
+
+    def __init__(self, measurements, backend=None, samples=None, nshots=1000):
+        from . import get_backend
+
+        self.backend = backend or get_backend()
+        self.measurements = measurements
+        self.nshots = nshots
+        self.measured_qubits = tuple(q for m in measurements for q in m.target_qubits)
+        self.density_matrix = False
+        self.nqubits = None
+        self._state = None
+        self._probs = None
+        self._samples = None if samples is None else np.asarray(samples)
+        self._frequencies = None
+        if self._samples is not None:
+            for m in measurements:
+                idx = [self.measured_qubits.index(q) for q in m.target_qubits]
+                if hasattr(m, "result"):
+                    m.result.register_samples(self._samples[:, idx])
+
+    def state(self, numpy: bool = False):
+        raise RuntimeError("repeated execution keeps no final state: use samples or frequencies")
+
+    def probabilities(self, qubits=None):
+        n = len(self.measured_qubits)
+        qubits = self.measured_qubits if qubits is None else tuple(qubits)
+        idx = [self.measured_qubits.index(q) for q in qubits]
+        p = np.zeros(2 ** len(idx))
+        for k, v in self.frequencies(binary=False).items():
+            bits = [(k >> (n - 1 - i)) & 1 for i in idx]
+            p[int("".join(map(str, bits)) or "0", 2)] += v
+        return p / self.nshots
+
+    def __str__(self):
+        return f"MeasurementOutcomes(nshots={self.nshots}, qubits={self.measured_qubits})"

@@ -183,6 +183,30 @@ def main(src: str = DEFAULT_SRC):
         grads.append(parameter_shift(c, ham, parameter_index=i))
     out["vqe4_psr_grads"] = np.array(grads)
 
+    # 8. state collapse (Backend.collapse_state, ascending qubit lists as
+    #    M.apply passes them) and an expectation value from frequencies
+    #    (exp_value_diagonal_observable_symbolic_from_samples)
+    backend = qibo.get_backend()
+    st = out["brick8_c128"]
+    collapse_cases = [([2], 1), ([0, 5], 2), ([1, 3, 7], 5), ([4, 6], 0)]
+    for i, (qs, k) in enumerate(collapse_cases):
+        out[f"collapse_{i}"] = backend.collapse_state(st.copy(), qs, np.array([k]), 8)
+        out[f"collapse_{i}_unnorm"] = backend.collapse_state(st.copy(), qs, np.array([k]), 8, normalize=False)
+    meta["collapse_cases"] = [[list(q), k] for q, k in collapse_cases]
+    fs = {"freq": {"0110": 37, "1011": 12, "0001": 80, "1111": 5, "0100": 21}, "qubit_map": [3, 0, 5, 2],
+          "terms_qubits": [[3], [0, 5], [2, 3, 0], [5, 2]], "coefs": [0.5, -1.25, 0.75, 2.0], "constant": 0.3}
+
+    class _Frequencies:
+        def frequencies(self):
+            return dict(fs["freq"])
+
+    c = Circuit(1)
+    c._final_state = _Frequencies()
+    out["fromsamples_value"] = np.array(backend.exp_value_diagonal_observable_symbolic_from_samples(
+        c, 6, [tuple(q) for q in fs["terms_qubits"]], fs["coefs"], nshots=1, qubit_map=fs["qubit_map"],
+        constant=fs["constant"]))
+    meta["fromsamples"] = fs
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **out)
     with open(os.path.join(HERE, "reference_vectors.json"), "w") as f:
         json.dump(meta, f, indent=1)

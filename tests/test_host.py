@@ -164,3 +164,24 @@ def test_qibo_plugin_registration():
     mod = importlib.import_module("qibo-gb300".replace("-", "_"))
     assert mod is qibo_gb300
     assert callable(construct_backend)
+
+
+def test_measurement_semantics_of_the_standalone_circuit():
+    """models/circuit.py:658-689: basis rotations go in before the
+    measurement; a gate on a measured qubit turns that measurement into a
+    collapsing one, which makes the circuit run shot by shot."""
+    from qibo_gb300 import Circuit, gates
+
+    c = Circuit(3)
+    c.add(gates.H(0))
+    m = gates.M(0, 2, basis=[gates.X, "Y"])
+    c.add(m)
+    names = [type(g).__name__ for g in c.queue]
+    assert names == ["H", "H", "Unitary", "M"] and c.measurements == [m] and not c.repeated_execution
+    np.testing.assert_allclose(c.queue[2].matrix(), ref.basis_rotation("Y"), atol=1e-15)
+    c.add(gates.CNOT(2, 1))
+    assert m.collapse and c.has_collapse and c.repeated_execution and c.measurements == []
+    c.add(gates.M(1))
+    assert len(c.measurements) == 1
+    with pytest.raises(NotImplementedError):
+        gates.M(0, p0=0.1)

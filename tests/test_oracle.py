@@ -135,3 +135,23 @@ def test_oracle_reference_derivative_kat(scale, kat):
 
     g = ref.parameter_shift_grad(build, 1, p, ["Z"], [(0,)], [1.0], scale_factor=scale)
     np.testing.assert_allclose(g, kat, atol=1e-8)
+
+
+def test_oracle_collapse(gold):
+    """Backend.collapse_state (backends/abstract.py:3279-3304) against the
+    reference's own outputs, with and without normalisation."""
+    data, meta = gold
+    st = data["brick8_c128"]
+    for i, (qs, k) in enumerate(meta["collapse_cases"]):
+        np.testing.assert_allclose(ref.collapse_statevector(st, qs, k, 8), data[f"collapse_{i}"], atol=1e-15)
+        np.testing.assert_allclose(ref.collapse_statevector(st, qs, k, 8, normalize=False),
+                                   data[f"collapse_{i}_unnorm"], atol=1e-15)
+
+
+def test_oracle_expectation_from_frequencies(gold):
+    """exp_value_diagonal_observable_symbolic_from_samples (:2873-2926) on the
+    reference's frequency table."""
+    data, meta = gold
+    fs = meta["fromsamples"]
+    got = ref.exp_value_from_frequencies(fs["freq"], fs["terms_qubits"], fs["coefs"], fs["qubit_map"], fs["constant"])
+    assert abs(got - float(data["fromsamples_value"])) < 1e-15
