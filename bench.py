@@ -20,7 +20,7 @@ same circuit with its infidelity against the complex128 state, and a
 bounded sample of the serving stream (circuits/s, p50/p99).
 
 Other workloads (``--workload``): ``qft20``, ``vqe24``, ``serving``, ``tc5``,
-``memlimit``.  ``--impl reference`` times the reference's CPU algorithm (the
+``memlimit``, ``kernels`` (every hot-path call alone, with its roofline).  ``--impl reference`` times the reference's CPU algorithm (the
 numpy restatement in ``oracle/``, all host cores) on a bounded sample of the
 same workload.
 """
@@ -670,6 +670,139 @@ def run_tc5(args):
                       "hbm_peak_gbs": peak, "tc_wait_timeouts": flag.value, **out}))
 
 
+def run_kernels(args):
+    """Every hot-path call alone, on a dense random state of ``--nqubits``
+    qubits (default 30: 17.2 GB complex128, 8.6 GB complex64; inputs >> L2),
+    in both precisions: ``--warmup`` untimed calls, then ``--steps`` calls
+    timed with CUDA events on the launch stream.  Algorithmic bytes per call
+    (S = bytes per amplitude, N = 2^n): dense 1- and 2-qubit gates 2 N S; a
+    gate touching a fraction f of the amplitudes (CZ 1/4, CNOT and SWAP 1/2,
+    a doubly controlled gate 1/4) 2 f N S; a shared-memory pass 2 N S per
+    pass; probabilities N S + 2^m 8; norm N S; Pauli expectation N S per
+    distinct flip mask; collapse on k qubits 2 N S / 2^k + N S (the kept
+    slice is read twice, every amplitude written once); sampling
+    from probabilities N 8 + 8 per shot; sampling from the state N S + 8 per
+    shot; parity counts 8 per shot."""
+    from qibo_gb300 import _lib
+    from qibo_gb300._lib import check, int_array
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceArray, DeviceState
+    from qibo_gb300.serving import compile_brickwork, u3_matrices
+
+    n = args.nqubits
+    N = 2**n
+    peak = measured_peaks().get("hbm_gbs", 6800.0)
+    rng = np.random.default_rng(7)
+
+    def unitary(d):
+        q, _ = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))
+        return np.ascontiguousarray(q.astype(np.complex128)).view(np.float64).ravel()
+
+    u1, u2 = unitary(2), unitary(4)
+    cz = np.ascontiguousarray(np.diag([1, 1, 1, -1]).astype(np.complex128)).view(np.float64).ravel()
+    cx = np.ascontiguousarray(np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]],
+                                       dtype=np.complex128)).view(np.float64).ravel()
+    sw = np.ascontiguousarray(np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]],
+                                       dtype=np.complex128)).view(np.float64).ravel()
+    layer_ops, layer_coefs = compile_brickwork(n, 1, rng.uniform(0, 2 * np.pi, (1, n, 3)))
+    x_terms = n
+    out = {"workload": f"every hot-path call alone, n={n}, dense random state", "hbm_peak_gbs": peak,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    nshots = 1_000_000
+    for dtype, S in (("complex128", 16), ("complex64", 8)):
+        b = GB300Backend(dtype)
+        rt, lib, eng = b.rt, b.rt.lib, b.engine_gb
+        s = rt.stream
+        st = DeviceState(n, dtype)
+        code = st.code
+        check(lib.qgb_state_zero(st.ptr, n, code, s))
+        dense = [((q,), (), u3_matrices(rng.uniform(0, 2 * np.pi, 3))) for q in range(n)]
+        eng.apply_many(st, dense, blocked=True)
+        probs = DeviceArray((N,), np.float64, rt)
+        p10 = DeviceArray((1024,), np.float64, rt)
+        norm = DeviceArray((1,), np.float64, rt)
+        samples = DeviceArray((nshots,), np.int64, rt)
+        odd = DeviceArray((64,), np.int64, rt)
+        outcome = DeviceArray((1,), np.int64, rt)
+        rt.h2d(outcome.ptr, np.array([5], dtype=np.int64))
+        allq = int_array(range(n))
+        q10 = int_array(list(range(0, n, 2))[:10])  # 10 distinct qubits for every n >= 19
+        scratch = rt.scratch(max(lib.qgb_probs_scratch_bytes(n, n), lib.qgb_sample_scratch_bytes(n),
+                                 lib.qgb_sample_state_scratch_bytes(n), lib.qgb_norm_scratch_bytes(),
+                                 lib.qgb_expect_scratch_bytes(n, 2 * n)))
+        zz_x = [0] * n
+        zz_z = [(1 << i) | (1 << ((i + 1) % n)) for i in range(n)]
+        xs_x = [1 << i for i in range(n)]
+        xs_z = [0] * n
+        ones = _lib.double_array([1.0] * n)
+        masks = (C.c_uint64 * 64)(*[int(m) for m in rng.integers(1, 2**n, 64)])
+        npass = eng.count_passes(n, code, [((int(o["qubits"][0]),) if o["k"] == 1 else
+                                            (int(o["qubits"][0]), int(o["qubits"][1])), (),
+                                            layer_coefs[o["coef_offset"]:o["coef_offset"] + (8 if o["k"] == 1 else 32)]
+                                            .view(np.complex128).reshape((2, 2) if o["k"] == 1 else (4, 4)))
+                                           for o in layer_ops])
+
+        def gate(qs, ctrl, m):
+            return lambda: check(lib.qgb_apply_gate(st.ptr, n, code, int_array(qs), len(qs), int_array(ctrl),
+                                                    len(ctrl), m.ctypes.data_as(_lib.dp), s))
+
+        calls = [
+            ("dense 1q, qubit 0 (index bit n-1)", "k_1q_pairs", 2 * N * S, gate([0], [], u1)),
+            ("dense 1q, qubit n/2", "k_1q_pairs", 2 * N * S, gate([n // 2], [], u1)),
+            ("dense 1q, qubit n-1 (index bit 0, warp shuffles)", "k_1q_shfl", 2 * N * S, gate([n - 1], [], u1)),
+            ("dense 2q, qubits 3, n-5", "k_dense<2>", 2 * N * S, gate([3, n - 5], [], u2)),
+            ("CZ, qubits n/2, n/2+1 (diagonal on a quarter)", "k_phase", 2 * N * S // 4,
+             gate([n // 2, n // 2 + 1], [], cz)),
+            ("CNOT, qubits 2, n-2 (swap on a half)", "k_xlike", 2 * N * S // 2, gate([2, n - 2], [], cx)),
+            ("SWAP, qubits 1, n-3", "k_swap", 2 * N * S // 2, gate([1, n - 3], [], sw)),
+            ("U3 on qubit 5 controlled by qubits 1, 2", "k_1q_pairs (controlled)", 2 * N * S // 4, gate([5], [1, 2], u1)),
+            (f"one brickwork layer in shared-memory passes ({npass} passes)", "k_pass", npass * 2 * N * S,
+             lambda: check(lib.qgb_apply_circuit(st.ptr, n, code, layer_ops.ctypes.data_as(C.POINTER(_lib.QgbOp)),
+                                                 len(layer_ops), layer_coefs.ctypes.data_as(_lib.dp),
+                                                 _lib.QGB_PLAN_BLOCKED, s))),
+            ("probabilities, all qubits", "k_probs_all", N * S + N * 8,
+             lambda: check(lib.qgb_probabilities(st.ptr, n, code, allq, n, probs.ptr, scratch, s))),
+            ("probabilities, 10 qubits", "k_probs_*", N * S + 1024 * 8,
+             lambda: check(lib.qgb_probabilities(st.ptr, n, code, q10, 10, p10.ptr, scratch, s))),
+            ("norm", "k_norm_part + k_final_sum", N * S,
+             lambda: check(lib.qgb_norm2(st.ptr, n, code, norm.ptr, scratch, s))),
+            (f"Z Z expectation, {n} terms (one flip mask)", "k_expect_diag", N * S,
+             lambda: check(lib.qgb_expect_pauli(st.ptr, n, code, (C.c_uint64 * n)(*zz_x), (C.c_uint64 * n)(*zz_z),
+                                                ones, n, norm.ptr, scratch, s))),
+            (f"X expectation, {x_terms} terms ({x_terms} flip masks)", "k_expect_flip", x_terms * N * S,
+             lambda: check(lib.qgb_expect_pauli(st.ptr, n, code, (C.c_uint64 * n)(*xs_x), (C.c_uint64 * n)(*xs_z),
+                                                ones, n, norm.ptr, scratch, s))),
+            ("collapse on 3 qubits", "k_collapse_norm + k_collapse_apply", N * S // 8 + N * S // 8 + N * S,
+             lambda: check(lib.qgb_collapse(st.ptr, n, code, int_array([0, n // 2, n - 1]), 3, outcome.ptr, 1,
+                                            scratch, s))),
+            (f"{nshots} shots from the 2^n probabilities", "k_chunk_sums + k_scan_* + k_draw", N * 8 + nshots * 8,
+             lambda: check(lib.qgb_sample(probs.ptr, n, nshots, 11, samples.ptr, None, scratch, s))),
+            (f"{nshots} shots straight from the state", "k_state_chunk_sums + k_scan_* + k_draw_state",
+             N * S + nshots * 8,
+             lambda: check(lib.qgb_sample_state(st.ptr, n, code, nshots, 12, samples.ptr, scratch, s))),
+            (f"parity counts, {nshots} shots x 64 terms", "k_parity", nshots * 8,
+             lambda: check(lib.qgb_parity_counts(samples.ptr, nshots, masks, 64, odd.ptr, s))),
+        ]
+        ev = Events(lib)
+        check(lib.qgb_probabilities(st.ptr, n, code, allq, n, probs.ptr, scratch, s))
+        rows = []
+        for name, kern, nbytes, call in calls:
+            if name.startswith("collapse"):
+                eng.apply_many(st, dense, blocked=True)  # every collapse starts from a dense state
+            for _ in range(args.warmup):
+                call()
+            ev.start(s)
+            for _ in range(args.steps):
+                call()
+            ms = ev.stop_ms(s) / args.steps
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            rows.append({"call": name, "kernels": kern, "ms": round(ms, 4), "bytes": int(nbytes),
+                         "GB/s": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 3)})
+        out[dtype] = rows
+        del st, probs, samples
+    print(json.dumps(out))
+
+
 def run_memlimit(args):
     """33-qubit complex128 (137 GB) and 34-qubit complex64 (137 GB): QFT then
     a depth-10 U3+CZ brickwork in shared-memory passes, 1e7 shots drawn
@@ -731,7 +864,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="brickwork",
-                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5"])
+                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
@@ -745,7 +878,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
-            "memlimit": run_memlimit, "tc5": run_tc5}[args.workload](args)
+            "memlimit": run_memlimit, "tc5": run_tc5, "kernels": run_kernels}[args.workload](args)
 
 
 if __name__ == "__main__":

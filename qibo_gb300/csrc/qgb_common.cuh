@@ -58,6 +58,20 @@ __host__ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 a
   return make_double2(fma(-a.y, b.y, fma(a.x, b.x, acc.x)), fma(a.y, b.x, fma(a.x, b.y, acc.y)));
 }
 
+// Exact float -> double without the conversion instruction, which GB300
+// issues on its slow FP64 pipe: rebias the exponent and widen the mantissa
+// with integer operations (normal numbers and zeros); subnormals,
+// infinities and NaNs take the conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  if (e - 1u < 0xFEu)
+    return __longlong_as_double((long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
+  if ((u << 1) == 0) return __longlong_as_double((long long)sign);
+  return (double)f;
+}
+
 struct TC64 {
   typedef float2 S;   // storage
   typedef float2 V;   // value computed on
@@ -69,11 +83,26 @@ struct TC64 {
   __device__ static void store(S* p, i64 i, V v) { p[i] = v; }
   __device__ static V mul(V a, V b) { return cmul(a, b); }
   __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
-  __device__ static double abs2(V a) { return (double)a.x * a.x + (double)a.y * a.y; }
-  __device__ static V scale(V a, double s) { return make_float2((float)(a.x * s), (float)(a.y * s)); }
+  // x^2 and y^2 of floats are exact in FP64, so one rounding in all: the
+  // FP64 pipe sees one multiply and one FMA, no conversions
+  __device__ static double abs2(V a) {
+    const double x = f2d_exact(a.x), y = f2d_exact(a.y);
+    return ::fma(x, x, y * y);
+  }
+  // acc + |a|^2 as two FMAs (two FP64 operations instead of three)
+  __device__ static double acc2(double acc, V a) {
+    const double x = f2d_exact(a.x), y = f2d_exact(a.y);
+    return ::fma(x, x, ::fma(y, y, acc));
+  }
+  // in FP32 with the factor rounded once (relative error <= 2^-23, the
+  // precision of the stored floats), off the FP64 pipe
+  __device__ static V scale(V a, double s) {
+    const float f = (float)s;
+    return make_float2(a.x * f, a.y * f);
+  }
   __device__ static V neg(V a) { return make_float2(-a.x, -a.y); }
-  __device__ static double re(V a) { return a.x; }
-  __device__ static double im(V a) { return a.y; }
+  __device__ static double re(V a) { return f2d_exact(a.x); }
+  __device__ static double im(V a) { return f2d_exact(a.y); }
 };
 
 struct TC128 {
@@ -88,6 +117,7 @@ struct TC128 {
   __device__ static V mul(V a, V b) { return cmul(a, b); }
   __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
   __device__ static double abs2(V a) { return fma_d(a.x, a.x, a.y * a.y); }
+  __device__ static double acc2(double acc, V a) { return ::fma(a.x, a.x, ::fma(a.y, a.y, acc)); }
   __device__ static double fma_d(double a, double b, double c) { return ::fma(a, b, c); }
   __device__ static V scale(V a, double s) { return make_double2(a.x * s, a.y * s); }
   __device__ static V neg(V a) { return make_double2(-a.x, -a.y); }

@@ -121,6 +121,37 @@ __global__ void __launch_bounds__(256) k_phase(typename T::S* __restrict__ psi, 
   }
 }
 
+// The unit phases -1, i and -i (CZ, S, SDG and their controlled forms):
+// sign flips and a swap of the real and imaginary parts, with integer
+// operations, so the kernel never touches GB300's slow FP64 pipe.
+__device__ __forceinline__ double flip_sign(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ float flip_sign(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000u); }
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_phase_unit(S* __restrict__ psi, i64 count, BitInsert bi, i64 mask,
+                                                    int mode) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
+    const i64 i = insert_zeros(t, bi) | mask;
+    S v = psi[i];
+    if (mode == 1) {  // -1
+      v.x = flip_sign(v.x);
+      v.y = flip_sign(v.y);
+    } else if (mode == 2) {  // i: (x, y) -> (-y, x)
+      const auto x = v.x;
+      v.x = flip_sign(v.y);
+      v.y = x;
+    } else {  // -i: (x, y) -> (y, -x)
+      const auto x = v.x;
+      v.x = v.y;
+      v.y = flip_sign(x);
+    }
+    psi[i] = v;
+  }
+}
+
 // diagonal k-qubit gate with controls: amplitude *= d[target bits]
 template <typename T>
 struct DiagVec { typename T::V d[32]; };
@@ -257,6 +288,12 @@ int launch_phase(void* state, int n, const std::vector<int>& bits, zd ph, cudaSt
   const i64 count = (i64)1 << (n - (int)bits.size());
   int blocks;
   grid_for(count, 256, &blocks);
+  const int mode = ph == zd(-1.0, 0.0) ? 1 : ph == zd(0.0, 1.0) ? 2 : ph == zd(0.0, -1.0) ? 3 : 0;
+  if (mode) {
+    k_phase_unit<typename T::S><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(bits), mode);
+    QGB_LAUNCH_CHECK("k_phase_unit");
+    return QGB_OK;
+  }
   k_phase<T><<<blocks, 256, 0, s>>>((typename T::S*)state, count, bi, mask_of(bits), T::coef(ph.real(), ph.imag()));
   QGB_LAUNCH_CHECK("k_phase");
   return QGB_OK;

@@ -15,6 +15,7 @@
 //    :2946-3054): one pass per distinct X/Y flip mask covering all terms
 //    that share it, instead of one einsum pass per term.
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(256) k_probs_thread(const typename T::S* __res
     i64 base = 0;
     for (int b = 0; b < g.nq; ++b) base |= ((j >> b) & 1) << g.mpos[b];
     double acc = 0.0;
-    for (i64 r = 0; r < nr; ++r) acc += T::abs2(T::load(psi, base | deposit(r, g.upos, g.u)));
+    for (i64 r = 0; r < nr; ++r) acc = T::acc2(acc, T::load(psi, base | deposit(r, g.upos, g.u)));
     out[j] = acc;
   }
 }
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(256) k_probs_block(const typename T::S* __rest
   for (i64 r = r0 + threadIdx.x; r < r0 + per_part; r += blockDim.x) {
     // unmeasured index r -> amplitude index: insert zeros at measured positions
     const i64 idx = insert_zeros_n(r, g.msorted, g.nq) | base;
-    acc += T::abs2(T::load(psi, idx));
+    acc = T::acc2(acc, T::load(psi, idx));
   }
   acc = block_sum256(acc);
   if (threadIdx.x == 0) dst[blockIdx.x] = acc;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(256) k_norm_part(const typename T::S* __restri
                                                    double* __restrict__ part) {
   double acc = 0.0;
   const i64 stride = (i64)gridDim.x * blockDim.x;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) acc += T::abs2(T::load(psi, i));
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) acc = T::acc2(acc, T::load(psi, i));
   acc = block_sum256(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(256) k_state_chunk_sums(const typename T::S* _
   for (i64 c = blockIdx.x * (i64)blockDim.x + threadIdx.x; c < nchunks; c += stride) {
     double acc = 0.0;
     const i64 e = imin64(N, (c + 1) * QGB_CHUNK);
-    for (i64 i = c * QGB_CHUNK; i < e; ++i) acc += T::abs2(T::load(psi, i));
+    for (i64 i = c * QGB_CHUNK; i < e; ++i) acc = T::acc2(acc, T::load(psi, i));
     chunk[c] = acc;
   }
 }
@@ -414,10 +415,10 @@ __global__ void __launch_bounds__(256) k_draw_state(const typename T::S* __restr
     const i64 b = lo * QGB_CHUNK, e = imin64(N, b + QGB_CHUNK);
     i64 pick = -1, last_nz = -1;
     for (i64 i = b; i < e; ++i) {
-      const double p = T::abs2(T::load(psi, i));
-      if (p > 0.0) {
+      const typename T::V v = T::load(psi, i);
+      if (T::abs2(v) > 0.0) {
         last_nz = i;
-        run += p;
+        run = T::acc2(run, v);  // the chunk sums' operation (zeros add exactly nothing there)
         if (run > target) { pick = i; break; }
       }
     }
@@ -547,14 +548,21 @@ int qgb_philox_fill(uint32_t* out, int64_t n4, uint32_t c2, uint32_t c3, uint32_
 struct TermSet {
   int nterms;
   u64 zmask[QGB_TERMS_PER_LAUNCH];   // amplitude-index bit masks
-  double coef[QGB_TERMS_PER_LAUNCH];
-  int ny[QGB_TERMS_PER_LAUNCH];      // number of Y factors
+  double coef[QGB_TERMS_PER_LAUNCH]; // diagonal: c_t; flip: c_t f_t (see k_expect_flip)
+  // diagonal terms on 2^10 amplitudes or more: terms sorted by m = index
+  // bits 5..9 of their mask, [mstart[m], mstart[m+1]) having that m
+  uint32_t mused;
+  int mstart[33];
+  // flip terms: bit k set when term k uses Im(conj(psi_i) psi_j), else Re
+  uint32_t use_im_lo, use_im_hi;
+  int any_re, any_im;
 };
 
 // Terms with no X/Y factor: sum_i |psi_i|^2 * sum_t c_t (-1)^popc(i & z_t)
+// (states of fewer than 2^10 amplitudes).
 template <typename T>
-__global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __restrict__ psi, i64 N, TermSet ts,
-                                                     double* __restrict__ part) {
+__global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __restrict__ psi, i64 N,
+                                                     const __grid_constant__ TermSet ts, double* __restrict__ part) {
   double acc = 0.0;
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
@@ -567,12 +575,62 @@ __global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// The same on runs of 2^10 amplitudes, one per warp: lane l takes amplitudes
+// base + l + 32 k, k < 32 (coalesced), so k spans index bits 5..9.  With
+// p_k = |psi|^2 and S the Walsh-Hadamard transform of p over k
+// (S[m] = sum_k (-1)^popc(k & m) p_k, five butterfly stages), term t adds
+// c_t (-1)^popc(base & z_t) S[m_t] for the run, m_t = index bits 5..9 of
+// z_t: about 8 FP64 operations per amplitude whatever the number of terms,
+// against one per term and amplitude (GB300's FP64 pipe, not HBM, bounds
+// these reductions).
+template <typename T>
+__global__ void __launch_bounds__(256) k_expect_diag_wht(const typename T::S* __restrict__ psi, i64 nruns,
+                                                         const __grid_constant__ TermSet ts,
+                                                         double* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const i64 warp = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+  const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (i64 w = warp; w < nruns; w += nwarps) {
+    const i64 base = (w << 10) | lane;
+    double p[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) p[k] = T::abs2(T::load(psi, base | ((i64)k << 5)));
+#pragma unroll
+    for (int h = 1; h < 32; h <<= 1) {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        if ((k & h) == 0) {
+          const double a = p[k], b = p[k | h];
+          p[k] = a + b;
+          p[k | h] = a - b;
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 32; ++m) {
+      if (!((ts.mused >> m) & 1)) continue;
+      double cm = 0.0;
+      for (int t = ts.mstart[m]; t < ts.mstart[m + 1]; ++t)
+        cm += (__popcll((u64)base & ts.zmask[t]) & 1) ? -ts.coef[t] : ts.coef[t];
+      acc = fma(cm, p[m], acc);
+    }
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
 // Terms sharing flip mask x (highest set bit hb): for each pair (i, j = i^x)
 // with bit hb of i clear, q = conj(psi_i) psi_j and the term adds
-// c * Re(i^ny * (s_j q + s_i conj(q))), s_k = (-1)^popc(k & z).
+// c Re(i^ny (s_j q + s_i conj(q))), s_k = (-1)^popc(k & z).  Since
+// s_j = s_i (-1)^ny (the bits of x & z are the term's Y factors), that is
+// f s_i Re(q) for even ny and f s_i Im(q) for odd ny, f = +2 / -2 by ny mod
+// 4: the host folds f into the coefficient and marks which part each term
+// needs, so a pair costs the parts its terms need and one FMA each.
 template <typename T>
 __global__ void __launch_bounds__(256) k_expect_flip(const typename T::S* __restrict__ psi, i64 npairs, int hb,
-                                                     u64 xmask, TermSet ts, double* __restrict__ part) {
+                                                     u64 xmask, const __grid_constant__ TermSet ts,
+                                                     double* __restrict__ part) {
   double acc = 0.0;
   const i64 stride = (i64)gridDim.x * blockDim.x;
   const i64 low = ((i64)1 << hb) - 1;
@@ -580,23 +638,21 @@ __global__ void __launch_bounds__(256) k_expect_flip(const typename T::S* __rest
     const i64 i = ((t >> hb) << (hb + 1)) | (t & low);
     const i64 j = i ^ (i64)xmask;
     const typename T::V a = T::load(psi, i), b = T::load(psi, j);
-    // q = conj(a) * b
-    const double qr = T::re(a) * T::re(b) + T::im(a) * T::im(b);
-    const double qi = T::re(a) * T::im(b) - T::im(a) * T::re(b);
-    for (int k = 0; k < ts.nterms; ++k) {
-      const double si = (__popcll((u64)i & ts.zmask[k]) & 1) ? -1.0 : 1.0;
-      const double sj = (__popcll((u64)j & ts.zmask[k]) & 1) ? -1.0 : 1.0;
-      // w = s_j q + s_i conj(q)
-      const double wr = (sj + si) * qr, wi = (sj - si) * qi;
-      double v;  // Re(i^ny * w)
-      switch (ts.ny[k] & 3) {
-        case 0: v = wr; break;
-        case 1: v = -wi; break;
-        case 2: v = -wr; break;
-        default: v = wi; break;
-      }
-      acc = fma(ts.coef[k], v, acc);
+    const double ar = T::re(a), ai = T::im(a), br = T::re(b), bi = T::im(b);
+    if (ts.nterms == 1) {
+      const double c = (__popcll((u64)i & ts.zmask[0]) & 1) ? -ts.coef[0] : ts.coef[0];
+      acc = ts.any_im ? fma(c, fma(ar, bi, -(ai * br)), acc) : fma(c, fma(ar, br, ai * bi), acc);
+      continue;
     }
+    double cre = 0.0, cim = 0.0;
+    for (int k = 0; k < ts.nterms; ++k) {
+      const double c = (__popcll((u64)i & ts.zmask[k]) & 1) ? -ts.coef[k] : ts.coef[k];
+      const uint32_t im = k < 32 ? (ts.use_im_lo >> k) & 1 : (ts.use_im_hi >> (k - 32)) & 1;
+      if (im) cim += c;
+      else cre += c;
+    }
+    if (ts.any_re) acc = fma(cre, fma(ar, br, ai * bi), acc);
+    if (ts.any_im) acc = fma(cim, fma(ar, bi, -(ai * br)), acc);
   }
   acc = block_sum256(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
@@ -651,17 +707,48 @@ int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t*
   for (auto& pg : plan) {
     const Group& g = pg.first;
     TermSet ts;
+    memset(&ts, 0, sizeof(ts));
     ts.nterms = (int)g.terms.size();
+    const u64 x = to_index_mask(g.x, n);
+    const bool wht = x == 0 && n >= 10;
+    std::vector<int> order(g.terms.begin(), g.terms.end());
+    if (wht)  // diagonal terms by their index bits 5..9
+      std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+        return ((to_index_mask(zmask[p], n) >> 5) & 31) < ((to_index_mask(zmask[q], n) >> 5) & 31);
+      });
     for (int k = 0; k < ts.nterms; ++k) {
-      const int t = g.terms[k];
-      const u64 z = to_index_mask(zmask[t], n), x = to_index_mask(xmask[t], n);
+      const int t = order[k];
+      const u64 z = to_index_mask(zmask[t], n);
+      const int ny = __builtin_popcountll(z & to_index_mask(xmask[t], n));
       ts.zmask[k] = z;
       ts.coef[k] = coef[t];
-      ts.ny[k] = __builtin_popcountll(z & x);
+      if (x != 0) {  // f = +2 for ny mod 4 in {0, 1}, -2 for {2, 3}; odd ny uses Im
+        ts.coef[k] = coef[t] * ((ny & 3) < 2 ? 2.0 : -2.0);
+        if (ny & 1) {
+          if (k < 32) ts.use_im_lo |= 1u << k;
+          else ts.use_im_hi |= 1u << (k - 32);
+          ts.any_im = 1;
+        } else {
+          ts.any_re = 1;
+        }
+      }
     }
-    const u64 x = to_index_mask(g.x, n);
+    if (wht) {
+      int k = 0;
+      for (int m = 0; m < 32; ++m) {
+        ts.mstart[m] = k;
+        while (k < ts.nterms && (int)((ts.zmask[k] >> 5) & 31) == m) ++k;
+        if (k > ts.mstart[m]) ts.mused |= 1u << m;
+      }
+      ts.mstart[32] = k;
+    }
     int blocks;
-    if (x == 0) {
+    if (wht) {
+      const i64 nruns = N >> 10;
+      grid_for(nruns * 32, 256, &blocks);
+      blocks = std::min(blocks, kExpectBlocksCap);
+      k_expect_diag_wht<T><<<blocks, 256, 0, s>>>((const S*)state, nruns, ts, part + used);
+    } else if (x == 0) {
       grid_for(N, 256, &blocks);
       blocks = std::min(blocks, kExpectBlocksCap);
       k_expect_diag<T><<<blocks, 256, 0, s>>>((const S*)state, N, ts, part + used);

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_collapse_norm(const typename T::S* __re
       const int p = a.sorted[j];
       idx = ((idx >> p) << (p + 1)) | (idx & ((((i64)1) << p) - 1));
     }
-    acc += T::abs2(T::load(psi, idx | (i64)value));
+    acc = T::acc2(acc, T::load(psi, idx | (i64)value));
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;

@@ -438,6 +438,32 @@ def test_pauli_strings_with_y_vs_oracle(backend):
     assert abs(got - want) < 1e-12
 
 
+@pytest.mark.parametrize("n", [10, 14])
+@pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-5)])
+def test_z_strings_vs_oracle(n, dtype, tol):
+    """Diagonal terms through the Walsh-Hadamard kernel (2^10 amplitudes or
+    more): 100 random Z strings, so two launches of at most 64 terms, with
+    masks on every index bit including bits 5..9 that the transform spans."""
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+    from qibo_gb300.engine import pauli_masks
+
+    b = GB300Backend(dtype)
+    psi = rand_state(n, 31)
+    rng = np.random.default_rng(8)
+    terms, qubits, coefs = [], [], []
+    for _ in range(100):
+        k = int(rng.integers(1, 6))
+        qs = tuple(int(x) for x in rng.choice(n, k, replace=False))
+        terms.append("Z" * k)
+        qubits.append(qs)
+        coefs.append(float(rng.normal()))
+    st = DeviceState.from_numpy(psi.astype(dtype), dtype)
+    want = ref.exp_value_observable_symbolic(np.asarray(st).astype(np.complex128), terms, qubits, coefs, n)
+    xs, zs = zip(*[pauli_masks(t, q) for t, q in zip(terms, qubits)])
+    assert abs(b.engine_gb.expect_pauli(st, xs, zs, coefs) - want) < tol
+
+
 def test_dense_expectation_vs_oracle(backend):
     n = 8
     psi = rand_state(n, 2)
