@@ -259,7 +259,10 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     p50/p99.  Both results are renormalised in FP64 and compared with the
     complex128 blocked result (infidelity 1 - |<psi128|psi64>|^2).
     ``c128_per_gate_ms`` is one run of the plain complex128 per-gate path
-    (IEEE FP64, one kernel per gate), the comparison point of the fused leg."""
+    (IEEE FP64, one kernel per gate), the comparison point of the fused leg;
+    ``c128_per_gate_double_float`` the same passes with dense gates in
+    double-float, with the per-gate-pass bandwidth (algorithmic bytes of
+    the gates over the device time)."""
     from qibo_gb300._lib import check
     from qibo_gb300.backend import GB300Backend, describe_gate
     from qibo_gb300.device import DeviceArray, DeviceState
@@ -316,22 +319,33 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
         tc_gbs = 2 * 2**n * 8 / (tc_ms * 1e-3) / 1e9
     tc_timeout = C.c_int(0)
     check(lib.qgb_tc_status(C.byref(tc_timeout)))
-    # plain complex128 per-gate path (state reused: the references above are done)
+    # plain complex128 per-gate path: IEEE FP64, one kernel per gate (state
+    # reused: the references above are done)
     check(lib.qgb_state_zero(state.ptr, n, state.code, rt.stream))
     ev.start(rt.stream)
-    eng.apply_many(state, descs, blocked=False)
+    eng.apply_many(state, descs, blocked=False, strict_fp64=True)
     ms_g = ev.stop_ms(rt.stream)
     del st64
-    # the fused complex128 result (tensor-core blocks) against that IEEE FP64
-    # per-gate result: 1 - |<psi_per_gate|psi_fused>|^2 in FP64
     st2 = DeviceState(n, "complex128")
+
+    def inf_vs_per_gate():  # 1 - |<psi_per_gate|psi>|^2 in FP64
+        check(lib.qgb_inner(state.ptr, st2.ptr, n, state.code, out.ptr, rt.scratch(lib.qgb_inner_scratch_bytes()),
+                            rt.stream))
+        re2, im2 = out.to_numpy()
+        return 1.0 - (re2 * re2 + im2 * im2)
+
+    # the same gates one pass each, dense gates in double-float
+    check(lib.qgb_state_zero(st2.ptr, n, st2.code, rt.stream))
+    ev.start(rt.stream)
+    eng.apply_many(st2, descs, blocked=False)
+    ms_df = ev.stop_ms(rt.stream)
+    inf_df = inf_vs_per_gate()
+    # the fused complex128 result (tensor-core blocks)
     check(lib.qgb_state_zero(st2.ptr, n, st2.code, rt.stream))
     eng.apply_many(st2, descs, blocked=True, fuse=True)
-    check(lib.qgb_inner(state.ptr, st2.ptr, n, state.code, out.ptr, rt.scratch(lib.qgb_inner_scratch_bytes()),
-                        rt.stream))
-    re2, im2 = out.to_numpy()
-    inf_128 = 1.0 - (re2 * re2 + im2 * im2)
+    inf_128 = inf_vs_per_gate()
     del st2
+    g128, _ = algorithmic_bytes(n, ndense, ncz, 16)
     g64, _ = algorithmic_bytes(n, ndense, ncz, 8)
     p50 = statistics.median(ms_f)
     p99 = ms_f[min(len(ms_f) - 1, int(np.ceil(0.99 * len(ms_f))) - 1)]
@@ -344,6 +358,12 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
                          "k_fused5_tc_gbs": tc_gbs, "k_fused5_tc_bytes_per_launch": 2 * 2**n * 8,
                          "p99_note": "p99 of 8 runs is the slowest run"},
             "c128_per_gate_ms": ms_g, "c128_unfused_passes_ms": ms_128b,
+            "c128_per_gate_double_float": {
+                "ms": ms_df, "GB/s": g128 / (ms_df * 1e-3) / 1e9,
+                "frac_of_measured_hbm": g128 / (ms_df * 1e-3) / 1e9 / measured_peaks().get("hbm_gbs", 6800.0),
+                "infidelity_vs_per_gate_fp64": inf_df,
+                "note": "one pass per gate; dense gates in double-float, the doubles split and joined with integer "
+                        "operations; CZ by sign flips"},
             "c128_fused_infidelity_vs_per_gate_fp64": inf_128,
             "fused_tc_speedup_vs_c128_per_gate": ms_g / p50}
 
@@ -746,7 +766,20 @@ def run_kernels(args):
             return lambda: check(lib.qgb_apply_gate(st.ptr, n, code, int_array(qs), len(qs), int_array(ctrl),
                                                     len(ctrl), m.ctypes.data_as(_lib.dp), s))
 
+        def circuit_gate(q):  # one dense 1q gate through qgb_apply_circuit, gate by gate
+            ops, coefs = compile_brickwork(n, 1, rng.uniform(0, 2 * np.pi, (1, n, 3)))
+            one = ops[q:q + 1].copy()
+            one["coef_offset"] = 0
+            c1 = np.ascontiguousarray(coefs[ops[q]["coef_offset"]:ops[q]["coef_offset"] + 8])
+            return lambda: check(lib.qgb_apply_circuit(st.ptr, n, code, one.ctypes.data_as(C.POINTER(_lib.QgbOp)), 1,
+                                                       c1.ctypes.data_as(_lib.dp), 0, s))
+
+        df = " in double-float" if dtype == "complex128" else ""
         calls = [
+            (f"dense 1q gate by gate{df}, qubit 0", "k_1q_pairs<DF128>" if df else "k_1q_pairs", 2 * N * S,
+             circuit_gate(0)),
+            (f"dense 1q gate by gate{df}, qubit n-1", "k_1q_shfl<DF128>" if df else "k_1q_shfl", 2 * N * S,
+             circuit_gate(n - 1)),
             ("dense 1q, qubit 0 (index bit n-1)", "k_1q_pairs", 2 * N * S, gate([0], [], u1)),
             ("dense 1q, qubit n/2", "k_1q_pairs", 2 * N * S, gate([n // 2], [], u1)),
             ("dense 1q, qubit n-1 (index bit 0, warp shuffles)", "k_1q_shfl", 2 * N * S, gate([n - 1], [], u1)),

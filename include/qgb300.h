@@ -100,11 +100,13 @@ int qgb_apply_swap(void* state, int nqubits, int dtype, int q0, int q1,
  * ``ops`` is an array of ``nops`` qgb_op records, ``coefs`` holds their
  * matrices (each op's ``coef_offset`` indexes doubles).  The engine plans
  * shared-memory passes that apply many gates per read+write of the state
- * when ``flags & QGB_PLAN_BLOCKED``, otherwise it runs gate by gate.
+ * when ``flags & QGB_PLAN_BLOCKED``, otherwise it runs gate by gate.  Gate
+ * by gate, complex128 dense gates of one or two qubits compute in
+ * double-float too (the doubles split and joined with integer operations),
+ * unless ``flags & QGB_PLAN_STRICT_FP64``; qgb_apply_gate keeps IEEE FP64.
  * Complex128 passes compute in double-float (two FP32 words per double,
  * about 48 significant bits) on the FP32 pipe unless
- * ``flags & QGB_PLAN_STRICT_FP64`` asks for IEEE FP64 arithmetic; the
- * gate-by-gate path always computes complex128 in IEEE FP64.  With
+ * ``flags & QGB_PLAN_STRICT_FP64`` asks for IEEE FP64 arithmetic.  With
  * QGB_PLAN_BLOCKED, uncontrolled 5-qubit dense blocks (fused gates) run on
  * the tensor cores (qgb_apply_fused5_tc; complex128 from 12 qubits) unless
  * ``flags & QGB_PLAN_NO_TC``. */

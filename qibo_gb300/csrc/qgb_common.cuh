@@ -59,17 +59,22 @@ __host__ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 a
 }
 
 // Exact float -> double without the conversion instruction, which GB300
-// issues on its slow FP64 pipe: rebias the exponent and widen the mantissa
-// with integer operations (normal numbers and zeros); subnormals,
-// infinities and NaNs take the conversion instruction.
+// issues on its slow FP64 pipe: integer operations only, on every path
+// (a fallback to the instruction would be predicated, i.e. executed for
+// every value).  Normal numbers rebias the exponent and widen the mantissa;
+// subnormals are normalised (top bit p of the mantissa m: exponent p + 874);
+// infinities and NaNs keep their payload.
 __device__ __forceinline__ double f2d_exact(float f) {
   const uint32_t u = __float_as_uint(f);
   const uint32_t e = (u >> 23) & 0xFFu;
+  const uint32_t m = u & 0x7FFFFFu;
   const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-  if (e - 1u < 0xFEu)
-    return __longlong_as_double((long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
-  if ((u << 1) == 0) return __longlong_as_double((long long)sign);
-  return (double)f;
+  const uint64_t de = e == 0xFFu ? 0x7FFull : (uint64_t)(e + 896u);
+  const uint64_t normal = (de << 52) | ((uint64_t)m << 29);
+  const int p = 31 - __clz(m | 1u);
+  const uint64_t sub = m == 0 ? 0ull
+                              : ((uint64_t)(p + 874) << 52) | (((uint64_t)m << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)(sign | (e != 0 ? normal : sub)));
 }
 
 struct TC64 {
@@ -83,6 +88,7 @@ struct TC64 {
   __device__ static void store(S* p, i64 i, V v) { p[i] = v; }
   __device__ static V mul(V a, V b) { return cmul(a, b); }
   __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
+  __device__ static V row2(V u0, V a0, V u1, V a1) { return cfma(u1, a1, cmul(u0, a0)); }
   // x^2 and y^2 of floats are exact in FP64, so one rounding in all: the
   // FP64 pipe sees one multiply and one FMA, no conversions
   __device__ static double abs2(V a) {
@@ -116,6 +122,7 @@ struct TC128 {
   __device__ static void store(S* p, i64 i, V v) { p[i] = v; }
   __device__ static V mul(V a, V b) { return cmul(a, b); }
   __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
+  __device__ static V row2(V u0, V a0, V u1, V a1) { return cfma(u1, a1, cmul(u0, a0)); }
   __device__ static double abs2(V a) { return fma_d(a.x, a.x, a.y * a.y); }
   __device__ static double acc2(double acc, V a) { return ::fma(a.x, a.x, ::fma(a.y, a.y, acc)); }
   __device__ static double fma_d(double a, double b, double c) { return ::fma(a, b, c); }

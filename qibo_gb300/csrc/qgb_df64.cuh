@@ -83,6 +83,91 @@ __device__ __forceinline__ cdf cdf_row(const cdf* u, const cdf* a) {
 
 __device__ __forceinline__ cdf cdf_mul(cdf x, cdf y) { return cdf_row<1>(&x, &y); }
 
+// ---------------------------------------------------------------------------
+// Per-gate complex128 kernels in double-float.  A gate pass reads and writes
+// every IEEE double once, so the conversions cannot be amortised over many
+// gates as in a shared-memory pass; they avoid the FP64 pipe instead.
+//
+// Split: hi = x with its mantissa truncated to 24 bits; the 29 remaining
+// mantissa bits r give lo = RN(r) * 2^(e - 1075), |lo| < ulp(hi), so
+// x - (hi + lo) is below 2^-47 |x| (for |x| >= 2^-100; below, lo is a
+// subnormal float and the error below 2^-149).  Integer operations, one
+// integer to float conversion and two multiplications by powers of two, on
+// every path: |x| < 2^-126 becomes 0, |x| >= 2^128 an infinity, NaN a NaN.
+__device__ __forceinline__ df df_split_int(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const uint32_t h = (uint32_t)(u >> 32), l = (uint32_t)u;
+  const uint32_t sign = h & 0x80000000u;
+  const int E = (int)((h >> 20) & 0x7FF);
+  const int fe = E - 896;  // float exponent field of hi
+  const uint32_t mant = ((h & 0xFFFFFu) << 3) | (l >> 29);
+  const bool nan = E == 0x7FF && ((h & 0xFFFFFu) | l) != 0;
+  uint32_t hib = sign | ((uint32_t)fe << 23) | mant;
+  hib = fe <= 0 ? sign : fe >= 255 ? (sign | 0x7F800000u | (nan ? 0x400000u : 0u)) : hib;
+  // 2^(E - 1075) as 2^(E - 1011) * 2^-64: the first factor is a normal float
+  // whenever hi is, and the second rounds lo into the subnormals gradually
+  const float p2 = (fe > 0 && fe < 255) ? __uint_as_float((uint32_t)(E - 884) << 23) : 0.f;
+  const float lo = __uint_as_float(__float_as_uint((__uint2float_rn(l & 0x1FFFFFFFu) * p2) * 5.42101086242752217e-20f) | sign);
+  return {__uint_as_float(hib), lo};
+}
+
+// The join's widening: hi and lo come out of df_renorm, so each is a zero or
+// a normal float, except a lo below 2^-126, which read as normal errs by less
+// than 2^-125; infinities and NaNs keep exponent 2047.
+__device__ __forceinline__ double f2d_join(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  const uint64_t de = e == 0xFFu ? 0x7FFull : (uint64_t)(e + 896u);
+  const uint64_t bits = (u << 1) == 0 ? 0ull : (de << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)(sign | bits));
+}
+
+// hi + lo rounded once to an IEEE double: both widen exactly with integer
+// operations; the one FP64 addition rounds.
+__device__ __forceinline__ double df_join(df a) { return f2d_join(a.hi) + f2d_join(a.lo); }
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  return df_renorm(s, e);
+}
+
+// Per-gate traits: double2 in HBM, cdf in registers (k_1q_pairs, k_1q_shfl).
+struct DF128 {
+  typedef double2 S;
+  typedef cdf V;
+  static constexpr int kind = QGB_C128;
+  static V coef(double re, double im) {
+    cdf c;
+    c.re = df_split(re);
+    c.im = df_split(im);
+    return c;
+  }
+  __device__ static V load(const S* p, i64 i) {
+    const double2 v = p[i];
+    cdf c;
+    c.re = df_split_int(v.x);
+    c.im = df_split_int(v.y);
+    return c;
+  }
+  __device__ static void store(S* p, i64 i, V v) { p[i] = make_double2(df_join(v.re), df_join(v.im)); }
+  __device__ static V mul(V a, V b) { return cdf_mul(a, b); }
+  // u0 a0 + u1 a1 as one error-free dot product per real output
+  __device__ static V row2(V u0, V a0, V u1, V a1) {
+    const cdf u[2] = {u0, u1}, a[2] = {a0, a1};
+    return cdf_row<2>(u, a);
+  }
+  __device__ static V fma(V a, V b, V acc) {
+    const cdf m = cdf_mul(a, b);
+    cdf r;
+    r.re = df_add(acc.re, m.re);
+    r.im = df_add(acc.im, m.im);
+    return r;
+  }
+};
+
 // Shared-memory pass traits: double2 in HBM, cdf in shared memory.
 struct TC128F {
   typedef double2 G;

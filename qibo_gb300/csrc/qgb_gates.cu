@@ -21,6 +21,7 @@
 #include <cstring>
 #include <vector>
 
+#include "qgb_df64.cuh"
 #include "qgb_plan.h"
 
 template <int K>
@@ -68,11 +69,11 @@ __global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ ps
     typename T::V a0 = T::load(psi, i0), a1 = T::load(psi, i0 + step);
     typename T::V c0, c1;
     if (has2) { c0 = T::load(psi, j0); c1 = T::load(psi, j0 + step); }
-    T::store(psi, i0, T::fma(u01, a1, T::mul(u00, a0)));
-    T::store(psi, i0 + step, T::fma(u11, a1, T::mul(u10, a0)));
+    T::store(psi, i0, T::row2(u00, a0, u01, a1));
+    T::store(psi, i0 + step, T::row2(u10, a0, u11, a1));
     if (has2) {
-      T::store(psi, j0, T::fma(u01, c1, T::mul(u00, c0)));
-      T::store(psi, j0 + step, T::fma(u11, c1, T::mul(u10, c0)));
+      T::store(psi, j0, T::row2(u00, c0, u01, c1));
+      T::store(psi, j0 + step, T::row2(u10, c0, u11, c1));
     }
   }
 }
@@ -86,6 +87,15 @@ __device__ __forceinline__ float2 shfl_xor_v(float2 v, int mask) {
 template <>
 __device__ __forceinline__ double2 shfl_xor_v(double2 v, int mask) {
   return make_double2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
+}
+template <>
+__device__ __forceinline__ cdf shfl_xor_v(cdf v, int mask) {
+  cdf r;
+  r.re.hi = __shfl_xor_sync(0xffffffffu, v.re.hi, mask);
+  r.re.lo = __shfl_xor_sync(0xffffffffu, v.re.lo, mask);
+  r.im.hi = __shfl_xor_sync(0xffffffffu, v.im.hi, mask);
+  r.im.lo = __shfl_xor_sync(0xffffffffu, v.im.lo, mask);
+  return r;
 }
 
 // dense 1-qubit gate, no controls, target bit < 5: each lane owns one
@@ -106,7 +116,7 @@ __global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi
     // in the loop together, so the full-mask shuffle is safe.
     typename T::V a = T::load(psi, i);
     typename T::V p = shfl_xor_v(a, 1 << b);
-    T::store(psi, i, T::fma(cp, p, T::mul(cs, a)));
+    T::store(psi, i, T::row2(cs, a, cp, p));
   }
 }
 
@@ -218,6 +228,12 @@ i64 mask_of(const std::vector<int>& bits) {
   return m;
 }
 
+// widest dense gate a traits type runs (double-float per-gate gates: 2 qubits)
+template <typename T>
+constexpr int kMaxDenseK = QGB_MAX_K;
+template <>
+constexpr int kMaxDenseK<DF128> = 2;
+
 template <typename T>
 int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
   const int k = (int)g.tbits.size();
@@ -253,7 +269,7 @@ int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
   int blocks;
   grid_for(ngroups, 256, &blocks);
 #define QGB_DENSE_CASE(KK)                                                                        \
-  case KK: {                                                                                      \
+  case KK: if constexpr (KK <= kMaxDenseK<T>) {                                                   \
     Offs<KK> off;                                                                                 \
     DenseMat<T, KK> dm;                                                                           \
     for (int m = 0; m < D; ++m) {                                                                 \
@@ -491,6 +507,13 @@ int qgb_launch_gateop(void* state, int n, int dtype, const GateOp& g, cudaStream
   return launch_any(state, n, dtype, g, (void*)s);
 }
 
+// A complex128 dense gate of at most 2 qubits in double-float (DF128): the
+// per-gate circuit path when IEEE FP64 is not asked for.  The FP64 pipe would
+// bound these gates at about a third of HBM bandwidth.
+namespace {
+bool df_gate(const GateOp& g) { return g.kind == GK_DENSE && !g.identity && g.tbits.size() <= 2; }
+}  // namespace
+
 extern "C" {
 
 int qgb_apply_gate(void* state, int nqubits, int dtype, const int* qubits, int k, const int* controls,
@@ -604,13 +627,14 @@ extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_
   if (flags & QGB_PLAN_BLOCKED)
     return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0,
                            (flags & QGB_PLAN_NO_TC) == 0, s);
+  const bool df = dtype == QGB_C128 && !(flags & QGB_PLAN_STRICT_FP64);
   for (int i = 0; i < nops; ++i) {
     const qgb_op& op = ops[i];
     GateOp g;
     st = qgb_classify(nqubits, op.qubits, op.k, op.controls, op.ncontrols, coefs + op.coef_offset, &g,
                       "qgb_apply_circuit");
     if (st) return st;
-    st = launch_any(state, nqubits, dtype, g, stream);
+    st = df && df_gate(g) ? launch_dense<DF128>(state, nqubits, g, s) : launch_any(state, nqubits, dtype, g, stream);
     if (st) return st;
   }
   return QGB_OK;

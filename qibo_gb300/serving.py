@@ -338,9 +338,9 @@ class Server:
         fl.buffers.append((st, fp))
         n = r.nqubits
         check(self.lib.qgb_state_zero(st, n, code, stream))
-        if self.one_at_a_time:
+        if self.one_at_a_time:  # the plain per-gate path: one kernel per gate, IEEE FP64 for complex128
             check(self.lib.qgb_apply_circuit(st, n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
-                                             0, stream))
+                                             _lib.QGB_PLAN_STRICT_FP64, stream))
         elif n >= self.fuse_min_qubits:
             check(self.lib.qgb_apply_circuit(st, n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
                                              _lib.QGB_PLAN_BLOCKED | _lib.QGB_PLAN_FUSE, stream))

@@ -504,3 +504,37 @@ def test_errors_are_exceptions(backend):
         backend.engine_gb.apply(st, [1, 1], np.eye(4))
     with pytest.raises(RuntimeError):
         backend.execute_circuit(make_circuit(40, []))  # 16 TiB: device OOM -> RuntimeError
+
+
+@pytest.mark.parametrize("n", [8, 14])
+def test_per_gate_double_float_vs_oracle(n):
+    """complex128 gate by gate (qgb_apply_circuit without QGB_PLAN_BLOCKED):
+    dense 1- and 2-qubit gates in double-float, the doubles split and joined
+    with integer operations.  Depth-30 brickwork plus random dense 2-qubit
+    gates (some controlled) against the FP64 oracle to 1e-12, and against the
+    IEEE FP64 per-gate path (QGB_PLAN_STRICT_FP64)."""
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+
+    b = GB300Backend("complex128")
+    ops = ref.brickwork_ops(n, 30, 40 + n)
+    rng = np.random.default_rng(n)
+    descs = [(q, (), ref.gate_matrix(name, p)) for name, q, p in ops]
+    for _ in range(12):
+        q = tuple(int(x) for x in rng.choice(n, 3, replace=False))
+        u, _ = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))
+        ctrl = (q[2],) if rng.random() < 0.5 else ()
+        descs.append((q[:2], ctrl, u))
+        ops.append(("__dense2", q, u, ctrl))
+    psi0 = rand_state(n, 70 + n)
+    want = psi0.copy()
+    for op in ops:
+        if op[0] == "__dense2":
+            _, q, u, ctrl = op
+            want = ref.apply_gate_controlled_by(want, u, ctrl, q[:2], n) if ctrl else ref.apply_gate(want, u, q[:2], n)
+        else:
+            want = ref.apply_gate(want, ref.gate_matrix(op[0], op[2]), op[1], n)
+    for strict in (False, True):
+        st = DeviceState.from_numpy(psi0)
+        b.engine_gb.apply_many(st, descs, blocked=False, strict_fp64=strict)
+        assert np.max(np.abs(np.asarray(st) - want)) < 1e-12, strict
