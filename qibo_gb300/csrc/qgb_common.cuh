@@ -100,11 +100,13 @@ struct TC64 {
     const double x = f2d_exact(a.x), y = f2d_exact(a.y);
     return ::fma(x, x, ::fma(y, y, acc));
   }
-  // in FP32 with the factor rounded once (relative error <= 2^-23, the
-  // precision of the stored floats), off the FP64 pipe
+  // off the FP64 pipe: the FP64 factor split once into floats hi + lo (the
+  // split is loop-invariant), each value rounded once by fma(x, hi, x lo), so
+  // the factor keeps about 48 bits and an FP64 renormalisation stays one to
+  // within the rounding of the stored floats
   __device__ static V scale(V a, double s) {
-    const float f = (float)s;
-    return make_float2(a.x * f, a.y * f);
+    const float hi = (float)s, lo = (float)(s - (double)hi);
+    return make_float2(fmaf(a.x, hi, a.x * lo), fmaf(a.y, hi, a.y * lo));
   }
   __device__ static V neg(V a) { return make_float2(-a.x, -a.y); }
   __device__ static double re(V a) { return f2d_exact(a.x); }
