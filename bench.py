@@ -838,9 +838,11 @@ def run_kernels(args):
 
 def run_memlimit(args):
     """33-qubit complex128 (137 GB) and 34-qubit complex64 (137 GB): QFT then
-    a depth-10 U3+CZ brickwork in shared-memory passes, 1e7 shots drawn
-    straight from the state, <sum_i Z_i Z_{i+1}> (open chain), and the
-    complex64 infidelity against complex128 at 33 qubits."""
+    a depth-10 U3+CZ brickwork with engine fusion into <= 5-qubit blocks
+    (the engine keeps the fused list when it has at most 11 ops per pass of
+    the unfused shared-memory plan), 1e7 shots drawn straight from the
+    state, <sum_i Z_i Z_{i+1}> (open chain), and the complex64 infidelity
+    against complex128 at 33 qubits."""
     from qibo_gb300 import QFT, Circuit
     from qibo_gb300._lib import check
     from qibo_gb300.backend import GB300Backend, describe_gate
@@ -858,23 +860,33 @@ def run_memlimit(args):
         descs = [describe_gate(g, b) for g in c.queue]
         code = 1 if dtype == "complex128" else 0
         npass = eng.count_passes(n, code, descs)
+        nfused, n5 = eng.fuse_stats(descs, n)
+        fused = nfused <= 11 * npass
+        nops = nfused if fused else npass  # state passes of the plan the engine runs
         st = DeviceState(n, dtype)
         ev = Events(lib)
         check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
         ev.start(rt.stream)
-        eng.apply_many(st, descs, blocked=True)
+        eng.apply_many(st, descs, blocked=True, fuse=True)
         gms = ev.stop_ms(rt.stream)
+        # complex64 results get the FP64 renormalisation the backend applies
+        # (3xTF32 blocks drift the norm by about 5e-7 each)
+        norm_before = eng.renormalize(st) if dtype == "complex64" else None
         samples = DeviceArray((10_000_000,), np.int64, rt)
         ev.start(rt.stream)
         check(lib.qgb_sample_state(st.ptr, n, st.code, 10_000_000, 33, samples.ptr,
                                    rt.scratch(lib.qgb_sample_state_scratch_bytes(n)), rt.stream))
         sms = ev.stop_ms(rt.stream)
+        t0 = time.perf_counter()
         zz = eng.expect_pauli(st, [0] * (n - 1), [(1 << i) | (1 << (i + 1)) for i in range(n - 1)], [1.0] * (n - 1))
+        zz_ms = (time.perf_counter() - t0) * 1e3
         S = 16 if dtype == "complex128" else 8
         key = f"n{n}_{dtype}"
-        res[key] = {"gates": len(descs), "state_passes": npass, "gate_ms": gms,
-                    "pass_gbs": npass * 2 * 2**n * S / (gms * 1e-3) / 1e9, "shots_1e7_ms": sms, "zz_open_chain": zz,
-                    "state_gb": 2**n * S / 1e9}
+        res[key] = {"gates": len(descs), "plan": "fused blocks" if fused else "shared-memory passes",
+                    "fused_ops": nfused, "fused_5q_blocks": n5, "unfused_passes": npass, "state_passes": nops,
+                    "gate_ms": gms, "pass_gbs": nops * 2 * 2**n * S / (gms * 1e-3) / 1e9, "shots_1e7_ms": sms,
+                    "zz_open_chain": zz, "zz_ms_host": zz_ms, "state_gb": 2**n * S / 1e9,
+                    "norm_before_renormalisation": norm_before}
         del samples
         if n == 33:
             keep[dtype] = st

@@ -121,7 +121,9 @@ typedef struct qgb_op {
 #define QGB_PLAN_STRICT_FP64 2
 #define QGB_PLAN_NO_TC 8       /* fused 5-qubit blocks in shared-memory passes instead of on the tensor cores */
 #define QGB_PLAN_FUSE 16       /* with QGB_PLAN_BLOCKED: fuse the gate list into blocks of <= 5 qubits first
-                                  (greedy forward scan, Circuit.fuse's role, models/circuit.py:954-1003) */
+                                  (greedy forward scan, Circuit.fuse's role, models/circuit.py:954-1003),
+                                  kept when it has at most 11 ops per pass of the unfused plan (circuits
+                                  of mostly diagonal gates, such as QFT, run faster unfused) */
 int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                       const double* coefs, int flags, void* stream);
 /* What QGB_PLAN_FUSE makes of a gate list (host only): the number of ops
