@@ -666,8 +666,36 @@ def run_tc5(args):
                 check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, qa, mp, rt.stream))
             ms = ev.stop_ms(rt.stream) / args.steps
             gbs = nbytes / (ms * 1e-3) / 1e9
-            res[name] = {"qubits": qs, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
+            kname = kernel
+            low = [n - 1 - q for q in qs if n - 1 - q < 4]
+            if dtype == "complex64" and n >= 12 and len(low) <= 2 and not {0, 1} <= set(low):
+                kname = "k_fused5_tcm"  # A in tensor memory
+            res[name] = {"qubits": qs, "kernel": kname, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
                          "tensor_tflops": flops * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
+        if dtype == "complex64" and n >= 12:
+            # both complex64 kernels on placements with 0-5 block qubits on
+            # index bits 0..4 (QIBO_GB300_TC64_KERNEL picks the kernel)
+            sweep = []
+            for bits in ([5, 10, 15, 20, 25], [0, 10, 15, 20, 25], [4, 10, 15, 20, 25], [3, 4, 12, 18, 24],
+                         [0, 2, 12, 18, 24], [2, 3, 4, 15, 25], [0, 2, 4, 15, 25], [0, 1, 12, 18, 24],
+                         [0, 1, 2, 15, 25], [1, 2, 3, 4, 20], [0, 1, 2, 3, 20], [0, 1, 2, 3, 4]):
+                bits = [min(x, n - 5 + i) if x >= 5 else x for i, x in enumerate(bits)]
+                qa = _lib.int_array([n - 1 - x for x in bits])
+                row = {"index_bits": bits}
+                for kname, pick in (("k_fused5_tcm", "tmem"), ("k_fused5_tc", "smem")):
+                    os.environ["QIBO_GB300_TC64_KERNEL"] = pick
+                    try:
+                        for _ in range(args.warmup):
+                            check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, qa, mp, rt.stream))
+                        ev.start(rt.stream)
+                        for _ in range(args.steps):
+                            check(lib.qgb_apply_fused5_tc(st.ptr, n, st.code, qa, mp, rt.stream))
+                        ms = ev.stop_ms(rt.stream) / args.steps
+                    finally:
+                        del os.environ["QIBO_GB300_TC64_KERNEL"]
+                    row[kname] = {"ms": ms, "frac_of_measured_hbm": nbytes / (ms * 1e-3) / 1e9 / peak}
+                sweep.append(row)
+            res["placement_sweep"] = sweep
         if dtype == "complex128":
             # a chain of 10 unitary blocks through qgb_apply_circuit: the state
             # is converted once to the fixed-point format (norm pass + 2

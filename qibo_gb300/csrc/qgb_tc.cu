@@ -32,10 +32,16 @@
 // access then covers 16 distinct 8-byte slots (one wavefront), except the
 // A write of a block with no qubit on index bits 0..3 (two).
 //
+// On full tiles most placements run k_fused5_tcm instead (below): A goes to
+// tensor memory from registers, with no shared-memory staging, which takes
+// a block from 0.69-0.74 to 0.83-0.96 of HBM bandwidth.
+//
 // The wait on the mbarrier is bounded: on timeout the kernel records an
 // error flag, waits once more (bounded) for the in-flight MMAs, frees its
 // tensor memory and returns.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "qgb_plan.h"
@@ -262,6 +268,169 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_N));
 }
 
+// The same product with A in tensor memory (states of 12 qubits or more,
+// blocks that tcm_fits accepts).  A warp's lanes are 32 consecutive group
+// rows; for a block with no qubit on index bits 0..4 those are index bits
+// 0..4, and every warp access is 256 contiguous bytes; with block qubits
+// there the lanes are strided and L1/L2 merge the sectors of a row's
+// columns, which costs little while a warp access spans at most 8 lines.
+// Each thread loads
+// the 16 amplitudes of its row in one column half straight into registers,
+// splits them and writes A_hi / A_lo to its own tensor-memory lane with
+// tcgen05.st; the MMAs read A from tensor memory and only B from shared
+// memory; the epilogue reads D back with tcgen05.ld and stores to the
+// addresses it loaded from.  That removes the A writes, A operand reads and
+// the staging buffer from shared memory, whose bandwidth bounds the kernel
+// above.  Tensor memory per CTA: D in columns 0..63, A_hi 64..127, A_lo
+// 128..191 (256 allocated, two CTAs per SM).
+#define TCM_COLS 256
+#define TCM_SMEM (2 * TC_B_BYTES)
+
+// Tile geometry: a tile is the 5 block bits plus the 7 lowest other index
+// bits.  Thread (warp w, lane l) holds group row 32 (w % 4) + l and block
+// columns 16 h .. 16 h + 15, h = w / 4; its amplitude j sits at
+// base(tile) + lanes[l] + rowhi[w % 4] + h * chi + clo[j].
+struct TcmGeom {
+  int nrest;
+  int rest[32];
+  i64 lanes[32];  // offsets of group-row bits 0..4
+  i64 rowhi[4];   // offsets of group-row bits 5, 6
+  i64 chi;       // offset of block column bit 4
+  i64 clo[16];   // offsets of block columns 0..15
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    k_fused5_tcm(float2* __restrict__ psi, i64 ntiles, const __grid_constant__ TcmGeom geo,
+                 const __grid_constant__ TcGate G, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t s_base = smem_u32(sm);
+  const uint32_t mb = smem_u32(&mbar);
+
+  for (int e = tid; e < TC_N * TC_K; e += TC_THREADS) {
+    const int n = e / TC_K, k = e % TC_K;
+    const int r = n >> 1, c = k >> 1;
+    float v;
+    if ((n & 1) == 0) v = (k & 1) == 0 ? G.ur[r][c] : -G.ui[r][c];
+    else v = (k & 1) == 0 ? G.ui[r][c] : G.ur[r][c];
+    const float h = tf32_head(v);
+    const uint32_t o = core_off(n, k, TC_B_LBO, TC_B_SBO);
+    *(float*)(sm + o) = h;
+    *(float*)(sm + TC_B_BYTES + o) = v - h;
+  }
+  if (tid == 0) {
+    abort_flag = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TCM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // B, written here, is read by the MMAs
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t IDESC = tc_idesc(TC_M, TC_N);
+  uint32_t phase = 0;
+  const int h = warp >> 2;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32 * h;
+  const int my_rest = lane < geo.nrest ? geo.rest[lane] : -1;
+  const i64 toff = geo.lanes[lane] + geo.rowhi[warp & 3] + (h ? geo.chi : 0);
+
+  float2 v[16];
+  i64 t = blockIdx.x;
+  i64 base = 0;
+  if (t < ntiles) {
+    base = tile_base(t, lane, my_rest);
+    const float2* src = psi + base + toff;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = src[geo.clo[j]];
+  }
+  for (; t < ntiles; t += gridDim.x) {
+    // registers -> A_hi, A_lo (columns 2c, 2c + 1 = re, im of element c)
+    {
+      float a[32];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        a[2 * j] = tf32_head(v[j].x);
+        a[2 * j + 1] = tf32_head(v[j].y);
+      }
+      tmem_st16(tlane + 64, a);
+      tmem_st16(tlane + 80, a + 16);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        a[2 * j] = v[j].x - a[2 * j];
+        a[2 * j + 1] = v[j].y - a[2 * j + 1];
+      }
+      tmem_st16(tlane + 128, a);
+      tmem_st16(tlane + 144, a + 16);
+      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    // prefetch the next tile while the MMAs run
+    const i64 tn = t + gridDim.x;
+    i64 nbase = 0;
+    if (tn < ntiles) {
+      nbase = tile_base(tn, lane, my_rest);
+      const float2* src = psi + nbase + toff;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = src[geo.clo[j]];
+    }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      uint32_t acc = 0;
+#pragma unroll
+      for (int s = 0; s < TC_K / 8; ++s) {
+        const uint64_t bhi = smem_desc(s_base + s * 2 * TC_B_LBO, TC_B_LBO, TC_B_SBO);
+        const uint64_t blo = smem_desc(s_base + TC_B_BYTES + s * 2 * TC_B_LBO, TC_B_LBO, TC_B_SBO);
+        const uint32_t as[3] = {tmem + 64 + 8 * s, tmem + 64 + 8 * s, tmem + 128 + 8 * s};
+        const uint64_t bs[3] = {bhi, blo, bhi};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem),
+              "r"(as[q]), "l"(bs[q]), "r"(IDESC), "r"(acc));
+          acc = 1;
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+                   : "memory");
+    }
+    if (tid == 0 && !mbar_wait(mb, phase)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) {
+      if (tid == 0) {
+        atomicExch(err, 1);
+        mbar_wait(mb, phase);
+      }
+      break;
+    }
+    phase ^= 1;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    float y[32];
+    tmem_ld16(tlane, y);
+    tmem_ld16(tlane + 16, y + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    float2* dst = psi + base + toff;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) dst[geo.clo[j]] = make_float2(y[2 * j], y[2 * j + 1]);
+    // D and A are rewritten next: every thread's tensor-memory reads are done
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    base = nbase;
+  }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCM_COLS));
+}
+
 namespace {
 int* g_tc_err = nullptr;
 }  // namespace
@@ -359,6 +528,50 @@ void block_perm(const int cbit[5], int idx[32]) {
   }
 }
 
+// Geometry of k_fused5_tcm for target bits tbits in a state of 12 qubits
+// or more.  Block column bit i is the i-th lowest target, as in make_geom,
+// so block_perm of make_geom's cbit applies.
+void make_geom_m(int n, const std::vector<int>& tbits, TcmGeom* geo) {
+  std::vector<int> sorted_t = tbits;
+  std::sort(sorted_t.begin(), sorted_t.end());
+  std::vector<int> grp;
+  for (int b = 0; b < n && (int)grp.size() < 7; ++b)
+    if (std::find(tbits.begin(), tbits.end(), b) == tbits.end()) grp.push_back(b);
+  for (int l = 0; l < 32; ++l) {
+    geo->lanes[l] = 0;
+    for (int i = 0; i < 5; ++i)
+      if ((l >> i) & 1) geo->lanes[l] += (i64)1 << grp[i];
+  }
+  for (int k = 0; k < 4; ++k)
+    geo->rowhi[k] = ((k & 1) ? (i64)1 << grp[5] : 0) + ((k & 2) ? (i64)1 << grp[6] : 0);
+  for (int j = 0; j < 16; ++j) {
+    geo->clo[j] = 0;
+    for (int i = 0; i < 4; ++i)
+      if ((j >> i) & 1) geo->clo[j] += (i64)1 << sorted_t[i];
+  }
+  geo->chi = (i64)1 << sorted_t[4];
+  geo->nrest = 0;
+  for (int b = 0; b < n; ++b)
+    if (std::find(tbits.begin(), tbits.end(), b) == tbits.end() && std::find(grp.begin(), grp.end(), b) == grp.end())
+      geo->rest[geo->nrest++] = b;
+}
+
+// k_fused5_tcm's warp accesses touch 2^(5 - u) 128-byte lines, u = index
+// bits 0..3 that are not block bits, and up to 32 sectors when index bits
+// 0 and 1 are both block bits.  Measured at n=30 (8.6 GB, 12 placements):
+// with at most 8 lines and 16 sectors it moves 0.83-0.96 of HBM bandwidth,
+// with more 0.31-0.57, against 0.69-0.74 for k_fused5_tc on every placement.
+bool tcm_fits(const std::vector<int>& tbits) {
+  int low4 = 0;
+  bool b0 = false, b1 = false;
+  for (int b : tbits) {
+    low4 += b < 4;
+    b0 |= b == 0;
+    b1 |= b == 1;
+  }
+  return low4 <= 2 && !(b0 && b1);
+}
+
 template <bool FULL>
 void set_tc_smem_attr() {
   static bool done = false;
@@ -390,7 +603,18 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
     }
   const i64 ntiles = (i64)1 << (n - geo->nbits);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
-  if (geo->nbits == 12) {
+  // QIBO_GB300_TC64_KERNEL=smem / tmem picks the kernel on full tiles
+  // (for comparisons); unset or anything else, tcm_fits decides
+  const char* pick = getenv("QIBO_GB300_TC64_KERNEL");
+  const bool use_tcm = pick && !strcmp(pick, "smem")   ? false
+                       : pick && !strcmp(pick, "tmem") ? true
+                                                       : tcm_fits(g.tbits);
+  if (geo->nbits == 12 && use_tcm) {
+    TcmGeom* gm = new TcmGeom();
+    make_geom_m(n, g.tbits, gm);
+    k_fused5_tcm<<<blocks, TC_THREADS, TCM_SMEM, s>>>((float2*)state, ntiles, *gm, *G, err);
+    delete gm;
+  } else if (geo->nbits == 12) {
     set_tc_smem_attr<true>();
     k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
   } else {

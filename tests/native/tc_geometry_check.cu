@@ -12,7 +12,8 @@
 // wavefront per half-warp without conflicts) and fails if any pattern needs
 // more than the layout promises: 2 per warp for the staging writes and
 // reads, 2 for A writes of blocks with a qubit on index bits 0..3, else 4.
-// No kernel is launched.
+// The tensor-memory variant k_fused5_tcm is replayed the same way with the
+// tables of make_geom_m.  No kernel is launched.
 #include <complex>
 #include <cstdio>
 #include <map>
@@ -43,6 +44,110 @@ static int wavefronts(const uint32_t* off) {
     total += m;
   }
   return total;
+}
+
+static cd block_row(const std::vector<zd>& U, const int idx[32], int r, const cd* x) {
+  cd acc = 0;
+  for (int k = 0; k < 32; ++k) {
+    const zd u = U[idx[r] * 32 + idx[k]];
+    acc += cd(u.real(), u.imag()) * x[k];
+  }
+  return acc;
+}
+
+// k_fused5_tcm on the CPU with the tables make_geom_m builds: thread (warp
+// w, lane l) loads its row's 16 amplitudes of column half w / 4, the
+// permuted block product runs per row, and each thread stores its outputs
+// to the addresses it loaded.  Every amplitude must be read and written
+// once and the result must equal the block applied directly.
+static int check_tcm(std::mt19937_64& rng) {
+  std::normal_distribution<double> nd;
+  int fails = 0;
+  for (int n = 12; n <= 16; ++n) {
+    for (int trial = 0; trial < 16; ++trial) {
+      std::vector<int> all(n);
+      for (int i = 0; i < n; ++i) all[i] = i;
+      std::shuffle(all.begin(), all.end(), rng);
+      std::vector<int> tb(all.begin(), all.begin() + 5);
+      if (trial == 0) tb = {n - 1, n - 2, n - 3, n - 4, n - 5};
+      if (trial == 1) tb = {4, 3, 2, 1, 0};
+      if (trial == 2) tb = {9, 0, 2, 6, 5};
+      std::vector<zd> U(1024);
+      for (auto& c : U) c = zd(nd(rng), nd(rng));
+      TcGeom* geo = new TcGeom();
+      TcmGeom* gm = new TcmGeom();
+      int cbit[5], idx[32];
+      make_geom(n, tb, geo, cbit);
+      block_perm(cbit, idx);
+      make_geom_m(n, tb, gm);
+      const i64 N = (i64)1 << n;
+      std::vector<cd> psi(N), out(N, cd(1e300, 0)), ref(N);
+      for (auto& x : psi) x = cd(nd(rng), nd(rng));
+      for (i64 i = 0; i < N; ++i) {
+        int bi = 0;
+        for (int jt = 0; jt < 5; ++jt) bi |= (int)((i >> tb[jt]) & 1) << (4 - jt);
+        if (bi) continue;
+        i64 id[32];
+        for (int b = 0; b < 32; ++b) {
+          id[b] = i;
+          for (int jt = 0; jt < 5; ++jt)
+            if ((b >> (4 - jt)) & 1) id[b] |= (i64)1 << tb[jt];
+        }
+        for (int r = 0; r < 32; ++r) {
+          cd acc = 0;
+          for (int c = 0; c < 32; ++c) acc += cd(U[r * 32 + c].real(), U[r * 32 + c].imag()) * psi[id[c]];
+          ref[id[r]] = acc;
+        }
+      }
+      std::vector<int> seen(N, 0), wrote(N, 0);
+      bool bad = gm->nrest != n - 12;
+      for (i64 t = 0; t < ((i64)1 << (n - 12)) && !bad; ++t) {
+        i64 base = 0;
+        for (int b = 0; b < gm->nrest; ++b) base |= ((t >> b) & 1) << gm->rest[b];
+        std::vector<cd> A(TC_M * 32);
+        std::vector<i64> addr(TC_M * 32, -1);
+        for (int w = 0; w < 8; ++w)
+          for (int l = 0; l < 32; ++l)
+            for (int j = 0; j < 16; ++j) {
+              const i64 gi = base + gm->lanes[l] + gm->rowhi[w & 3] + ((w >> 2) ? gm->chi : 0) + gm->clo[j];
+              const int row = 32 * (w & 3) + l, c = 16 * (w >> 2) + j;
+              if (gi < 0 || gi >= N) { bad = true; continue; }
+              seen[gi]++;
+              A[row * 32 + c] = psi[gi];
+              addr[row * 32 + c] = gi;
+            }
+        for (int row = 0; row < TC_M; ++row)
+          for (int r = 0; r < 32; ++r) {
+            const i64 gi = addr[row * 32 + r];
+            if (gi < 0) { bad = true; continue; }
+            wrote[gi]++;
+            out[gi] = block_row(U, idx, r, &A[row * 32]);
+          }
+      }
+      double err = 0, nrm = 0;
+      for (i64 i = 0; i < N; ++i) {
+        if (seen[i] != 1 || wrote[i] != 1) bad = true;
+        err = std::max(err, std::abs(out[i] - ref[i]));
+        nrm = std::max(nrm, std::abs(ref[i]));
+      }
+      if (bad || err > 1e-9 * nrm) {
+        ++fails;
+        printf("FAIL tensor-memory variant n=%d block bits %d,%d,%d,%d,%d err=%g bad=%d\n", n, tb[0], tb[1], tb[2],
+               tb[3], tb[4], err, (int)bad);
+      }
+      delete gm;
+      delete geo;
+    }
+  }
+  // placement rule: at most two block bits on index bits 0..3, not both 0 and 1
+  const bool rule_ok = tcm_fits({5, 10, 15, 20, 25}) && tcm_fits({0, 2, 12, 18, 24}) &&
+                       tcm_fits({2, 3, 4, 15, 25}) && !tcm_fits({0, 1, 12, 18, 24}) &&
+                       !tcm_fits({1, 2, 3, 4, 20}) && !tcm_fits({0, 1, 2, 3, 4});
+  if (!rule_ok) {
+    ++fails;
+    printf("FAIL tcm_fits placement rule\n");
+  }
+  return fails;
 }
 
 int main() {
@@ -170,6 +275,8 @@ int main() {
       delete geo;
     }
   }
-  printf("cases %d index failures %d bank-pattern failures %d\n", cases, fails, bank_fails);
-  return (fails || bank_fails) ? 1 : 0;
+  const int tcm_fails = check_tcm(rng);
+  printf("cases %d index failures %d bank-pattern failures %d; tensor-memory variant failures %d\n", cases, fails,
+         bank_fails, tcm_fails);
+  return (fails || bank_fails || tcm_fails) ? 1 : 0;
 }

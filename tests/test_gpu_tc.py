@@ -43,7 +43,13 @@ def _apply_tc(psi, qubits, u, dtype=np.complex64):
 
 
 @pytest.mark.parametrize("n,qubits", [(7, (2, 3, 4, 5, 6)), (10, (0, 1, 2, 3, 4)), (12, (11, 3, 7, 0, 5)),
-                                      (14, (9, 10, 11, 12, 13)), (16, (1, 15, 8, 4, 12))])
+                                      (14, (9, 10, 11, 12, 13)), (16, (1, 15, 8, 4, 12)),
+                                      # A in tensor memory: no block qubit on index bits 0..4, then
+                                      # strided lanes (index bits 0, 2 / 3, 4 in the block)
+                                      (12, (0, 1, 2, 3, 4)), (13, (7, 0, 2, 5, 6)), (16, (10, 0, 3, 6, 9)),
+                                      (20, (14, 2, 13, 7, 11)), (15, (14, 12, 7, 3, 0)), (18, (14, 13, 2, 9, 5)),
+                                      # shared-memory A on a full tile: index bits 0 and 1 in the block
+                                      (14, (13, 12, 5, 2, 0))])
 def test_fused5_tc_matches_oracle(n, qubits):
     rng = np.random.default_rng(n)
     psi = rng.normal(size=2**n) + 1j * rng.normal(size=2**n)
