@@ -362,8 +362,9 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
                 "ms": ms_df, "GB/s": g128 / (ms_df * 1e-3) / 1e9,
                 "frac_of_measured_hbm": g128 / (ms_df * 1e-3) / 1e9 / measured_peaks().get("hbm_gbs", 6800.0),
                 "infidelity_vs_per_gate_fp64": inf_df,
-                "note": "one pass per gate; dense gates in double-float, the doubles split and joined with integer "
-                        "operations; CZ by sign flips"},
+                "note": "one pass per gate; dense 1-qubit gates with 2 of 8 warps in IEEE FP64 and 6 in "
+                        "double-float (the doubles split and joined with integer operations), dense 2-qubit gates "
+                        "in double-float; CZ by sign flips"},
             "c128_fused_infidelity_vs_per_gate_fp64": inf_128,
             "fused_tc_speedup_vs_c128_per_gate": ms_g / p50}
 
@@ -802,12 +803,30 @@ def run_kernels(args):
             return lambda: check(lib.qgb_apply_circuit(st.ptr, n, code, one.ctypes.data_as(C.POINTER(_lib.QgbOp)), 1,
                                                        c1.ctypes.data_as(_lib.dp), 0, s))
 
-        df = " in double-float" if dtype == "complex128" else ""
+        def with_fp64_warps(w, fn):  # QIBO_GB300_DF_FP64_WARPS around one call
+            def run():
+                os.environ["QIBO_GB300_DF_FP64_WARPS"] = str(w)
+                try:
+                    fn()
+                finally:
+                    del os.environ["QIBO_GB300_DF_FP64_WARPS"]
+            return run
+
+        df = " (FP64 / double-float warps)" if dtype == "complex128" else ""
         calls = [
-            (f"dense 1q gate by gate{df}, qubit 0", "k_1q_pairs<DF128>" if df else "k_1q_pairs", 2 * N * S,
+            (f"dense 1q gate by gate{df}, qubit 0", "k_1q_pairs_mix" if df else "k_1q_pairs", 2 * N * S,
              circuit_gate(0)),
-            (f"dense 1q gate by gate{df}, qubit n-1", "k_1q_shfl<DF128>" if df else "k_1q_shfl", 2 * N * S,
+            (f"dense 1q gate by gate{df}, qubit n-1", "k_1q_shfl_mix" if df else "k_1q_shfl", 2 * N * S,
              circuit_gate(n - 1)),
+        ]
+        if dtype == "complex128":  # the share of FP64 warps per 8-warp block
+            for w in (0, 1, 2, 3, 4, 8):
+                calls.append((f"dense 1q gate by gate, qubit 0, {w}/8 warps in FP64", "k_1q_pairs_mix", 2 * N * S,
+                              with_fp64_warps(w, circuit_gate(0))))
+            for w in (0, 1, 3):
+                calls.append((f"dense 1q gate by gate, qubit n-1, {w}/8 warps in FP64", "k_1q_shfl_mix", 2 * N * S,
+                              with_fp64_warps(w, circuit_gate(n - 1))))
+        calls += [
             ("dense 1q, qubit 0 (index bit n-1)", "k_1q_pairs", 2 * N * S, gate([0], [], u1)),
             ("dense 1q, qubit n/2", "k_1q_pairs", 2 * N * S, gate([n // 2], [], u1)),
             ("dense 1q, qubit n-1 (index bit 0, warp shuffles)", "k_1q_shfl", 2 * N * S, gate([n - 1], [], u1)),

@@ -18,7 +18,9 @@
 // kernels.
 #include <algorithm>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "qgb_df64.cuh"
@@ -55,9 +57,8 @@ __global__ void __launch_bounds__(256) k_dense(typename T::S* __restrict__ psi, 
 // dense 1-qubit gate, no controls, target bit >= 5: independent pairs,
 // coalesced 16-byte (c128) / 8-byte (c64) accesses, two pairs per thread.
 template <typename T>
-__global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ psi, i64 npairs, int b,
-                                                  typename T::V u00, typename T::V u01,
-                                                  typename T::V u10, typename T::V u11) {
+__device__ __forceinline__ void pairs_body(typename T::S* __restrict__ psi, i64 npairs, int b, typename T::V u00,
+                                           typename T::V u01, typename T::V u10, typename T::V u11) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   const i64 lowmask = ((i64)1 << b) - 1;
   const i64 step = (i64)1 << b;
@@ -76,6 +77,31 @@ __global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ ps
       T::store(psi, j0 + step, T::row2(u10, c0, u11, c1));
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ psi, i64 npairs, int b,
+                                                  typename T::V u00, typename T::V u01,
+                                                  typename T::V u10, typename T::V u11) {
+  pairs_body<T>(psi, npairs, b, u00, u01, u10, u11);
+}
+
+// complex128 gate by gate, the two arithmetic pipes at once: the first nf64
+// warps of every block compute their pairs in IEEE FP64 (the FP64 pipe, 16
+// DFMA per pair), the others in double-float (FP32 and integer pipes).
+// Alone, the FP64 form is bound by GB300's FP64 rate and the double-float
+// form by instruction issue; sharing the pairs between them keeps both
+// pipes busy part of the time.  Which warp computes which pair does not depend on nf64, and
+// both forms are accurate to a few units in the last place of FP64.
+struct Coef1q {
+  cdf d[4];      // double-float u00, u01, u10, u11
+  double2 e[4];  // the same in FP64
+};
+
+__global__ void __launch_bounds__(256) k_1q_pairs_mix(double2* __restrict__ psi, i64 npairs, int b, int nf64,
+                                                      const __grid_constant__ Coef1q u) {
+  if ((int)(threadIdx.x >> 5) < nf64) pairs_body<TC128>(psi, npairs, b, u.e[0], u.e[1], u.e[2], u.e[3]);
+  else pairs_body<DF128>(psi, npairs, b, u.d[0], u.d[1], u.d[2], u.d[3]);
 }
 
 template <typename V>
@@ -103,9 +129,8 @@ __device__ __forceinline__ cdf shfl_xor_v(cdf v, int mask) {
 // (lane ^ 2^b) with a warp shuffle.  Requires N >= 32 and a whole number of
 // warps per window (the grid covers N exactly in warps).
 template <typename T>
-__global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi, i64 N, int b,
-                                                 typename T::V u00, typename T::V u01,
-                                                 typename T::V u10, typename T::V u11) {
+__device__ __forceinline__ void shfl_body(typename T::S* __restrict__ psi, i64 N, int b, typename T::V u00,
+                                          typename T::V u01, typename T::V u10, typename T::V u11) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   const bool hi = (lane >> b) & 1;
@@ -118,6 +143,21 @@ __global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi
     typename T::V p = shfl_xor_v(a, 1 << b);
     T::store(psi, i, T::row2(cs, a, cp, p));
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi, i64 N, int b,
+                                                 typename T::V u00, typename T::V u01,
+                                                 typename T::V u10, typename T::V u11) {
+  shfl_body<T>(psi, N, b, u00, u01, u10, u11);
+}
+
+// k_1q_shfl with the pipes shared as in k_1q_pairs_mix (warp-uniform split,
+// so every shuffle still sees a whole warp)
+__global__ void __launch_bounds__(256) k_1q_shfl_mix(double2* __restrict__ psi, i64 N, int b, int nf64,
+                                                     const __grid_constant__ Coef1q u) {
+  if ((int)(threadIdx.x >> 5) < nf64) shfl_body<TC128>(psi, N, b, u.e[0], u.e[1], u.e[2], u.e[3]);
+  else shfl_body<DF128>(psi, N, b, u.d[0], u.d[1], u.d[2], u.d[3]);
 }
 
 // multiply ``phase`` into every amplitude whose ``mask`` bits are all 1
@@ -228,6 +268,21 @@ i64 mask_of(const std::vector<int>& bits) {
   return m;
 }
 
+// Warps per 256-thread block that compute dense 1-qubit complex128 gates in
+// IEEE FP64 while the rest use double-float (k_1q_pairs_mix); the
+// QIBO_GB300_DF_FP64_WARPS variable (0-8) overrides it for comparisons.
+// Measured at n=30 (one pass, 34.4 GB): 0/8 8.30 ms, 2/8 7.56 ms, 3/8
+// 8.38 ms, 4/8 9.51 ms, 8/8 14.41 ms.  The pipes overlap only in part: with
+// 3/8 in FP64 each alone would take about 5.4 ms.
+int df_fp64_warps() {
+  const char* v = getenv("QIBO_GB300_DF_FP64_WARPS");
+  if (v && *v) {
+    const int w = atoi(v);
+    return w < 0 ? 0 : w > 8 ? 8 : w;
+  }
+  return 2;
+}
+
 // widest dense gate a traits type runs (double-float per-gate gates: 2 qubits)
 template <typename T>
 constexpr int kMaxDenseK = QGB_MAX_K;
@@ -250,6 +305,28 @@ int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
     const int b = g.tbits[0];
     typename T::V u00 = T::coef(M[0].real(), M[0].imag()), u01 = T::coef(M[1].real(), M[1].imag());
     typename T::V u10 = T::coef(M[2].real(), M[2].imag()), u11 = T::coef(M[3].real(), M[3].imag());
+    if constexpr (std::is_same<T, DF128>::value) {
+      Coef1q cu;
+      for (int m = 0; m < 4; ++m) {
+        cu.d[m] = DF128::coef(M[m].real(), M[m].imag());
+        cu.e[m] = TC128::coef(M[m].real(), M[m].imag());
+      }
+      const int nf64 = df_fp64_warps();
+      int blocks;
+      if (b < 5 && n >= 5) {
+        const i64 N = (i64)1 << n;
+        grid_for(N, 256, &blocks);
+        k_1q_shfl_mix<<<blocks, 256, 0, s>>>((double2*)state, N, b, nf64, cu);
+        QGB_LAUNCH_CHECK("k_1q_shfl_mix");
+        return QGB_OK;
+      }
+      if (b >= 5) {
+        grid_for((ngroups + 1) / 2, 256, &blocks);
+        k_1q_pairs_mix<<<blocks, 256, 0, s>>>((double2*)state, ngroups, b, nf64, cu);
+        QGB_LAUNCH_CHECK("k_1q_pairs_mix");
+        return QGB_OK;
+      }
+    }
     if (b < 5 && n >= 5) {
       const i64 N = (i64)1 << n;
       int blocks;

@@ -538,3 +538,13 @@ def test_per_gate_double_float_vs_oracle(n):
         st = DeviceState.from_numpy(psi0)
         b.engine_gb.apply_many(st, descs, blocked=False, strict_fp64=strict)
         assert np.max(np.abs(np.asarray(st) - want)) < 1e-12, strict
+    # dense 1-qubit gates share their pairs between FP64 and double-float
+    # warps; every share (all double-float to all FP64) meets the same bar
+    for w in ("0", "5", "8"):
+        os.environ["QIBO_GB300_DF_FP64_WARPS"] = w
+        try:
+            st = DeviceState.from_numpy(psi0)
+            b.engine_gb.apply_many(st, descs, blocked=False)
+        finally:
+            del os.environ["QIBO_GB300_DF_FP64_WARPS"]
+        assert np.max(np.abs(np.asarray(st) - want)) < 1e-12, w
