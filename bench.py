@@ -719,6 +719,51 @@ def run_tc5(args):
                       "hbm_peak_gbs": peak, "tc_wait_timeouts": flag.value, **out}))
 
 
+def run_fusion(args):
+    """The engine's fusion rule on both sides of its threshold: QFT (about
+    13-15 fused ops per unfused pass) and QFT + depth-10 brickwork (about 9)
+    at ``--nqubits`` in both precisions, each gate list run once as
+    shared-memory passes and once as fused blocks
+    (QIBO_GB300_FUSE_OPS_PER_PASS=0 / 100000), after one untimed run; CUDA
+    events on the launch stream.  The engine keeps the fused list at most
+    11 ops per pass."""
+    from qibo_gb300 import QFT
+    from qibo_gb300._lib import check
+    from qibo_gb300.backend import GB300Backend, describe_gate
+    from qibo_gb300.device import DeviceState
+
+    n = args.nqubits
+    rows = []
+    for dtype in ("complex64", "complex128"):
+        b = GB300Backend(dtype)
+        rt, eng, lib = b.rt, b.engine_gb, b.rt.lib
+        ev = Events(lib)
+        for name in ("QFT", "QFT + depth-10 brickwork"):
+            c = QFT(n)
+            if name != "QFT":
+                c.add(brickwork_gates(n, 10, n))
+            descs = [describe_gate(g, b) for g in c.queue]
+            npass = eng.count_passes(n, 1 if dtype == "complex128" else 0, descs)
+            nfused, n5 = eng.fuse_stats(descs, n)
+            st = DeviceState(n, dtype)
+            row = {"circuit": name, "dtype": dtype, "gates": len(descs), "unfused_passes": npass,
+                   "fused_ops": nfused, "fused_ops_per_pass": nfused / npass,
+                   "engine_plan": "fused" if nfused <= 11 * npass else "passes"}
+            for plan, v in (("passes_ms", "0"), ("fused_ms", "100000")):
+                os.environ["QIBO_GB300_FUSE_OPS_PER_PASS"] = v
+                try:
+                    check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+                    eng.apply_many(st, descs, blocked=True, fuse=True)
+                    ev.start(rt.stream)
+                    eng.apply_many(st, descs, blocked=True, fuse=True)
+                    row[plan] = ev.stop_ms(rt.stream)
+                finally:
+                    del os.environ["QIBO_GB300_FUSE_OPS_PER_PASS"]
+            del st
+            rows.append(row)
+    print(json.dumps({"workload": f"engine fusion rule, n={n}", "rows": rows}))
+
+
 def run_kernels(args):
     """Every hot-path call alone, on a dense random state of ``--nqubits``
     qubits (default 30: 17.2 GB complex128, 8.6 GB complex64; inputs >> L2),
@@ -956,7 +1001,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="brickwork",
-                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels"])
+                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels", "fusion"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
@@ -970,7 +1015,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
-            "memlimit": run_memlimit, "tc5": run_tc5, "kernels": run_kernels}[args.workload](args)
+            "memlimit": run_memlimit, "tc5": run_tc5, "kernels": run_kernels,
+            "fusion": run_fusion}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -680,8 +680,14 @@ extern "C" int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int no
                                int* npasses);  // qgb_blocked.cu
 
 // QGB_PLAN_FUSE keeps the fused list when it has at most this many ops per
-// pass of the unfused shared-memory plan
+// pass of the unfused shared-memory plan (QIBO_GB300_FUSE_OPS_PER_PASS
+// overrides it, for comparisons)
 static const int kFuseOpsPerPass = 11;
+
+static int fuse_ops_per_pass() {
+  const char* v = getenv("QIBO_GB300_FUSE_OPS_PER_PASS");
+  return v && *v ? atoi(v) : kFuseOpsPerPass;
+}
 
 extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_op* ops, int nops,
                                  const double* coefs, int flags, void* stream) {
@@ -711,7 +717,7 @@ extern "C" int qgb_apply_circuit(void* state, int nqubits, int dtype, const qgb_
     int npasses = 0;
     st = qgb_plan_passes(nqubits, dtype, ops, nops, coefs, &npasses);
     if (st) return st;
-    if ((long long)fops.size() <= kFuseOpsPerPass * (long long)npasses)
+    if ((long long)fops.size() <= fuse_ops_per_pass() * (long long)npasses)
       return qgb_run_blocked(state, nqubits, dtype, fops.data(), (int)fops.size(), fcoefs.data(),
                              (flags & QGB_PLAN_STRICT_FP64) != 0, (flags & QGB_PLAN_NO_TC) == 0, s);
     return qgb_run_blocked(state, nqubits, dtype, ops, nops, coefs, (flags & QGB_PLAN_STRICT_FP64) != 0,
