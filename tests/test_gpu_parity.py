@@ -548,3 +548,30 @@ def test_per_gate_double_float_vs_oracle(n):
         finally:
             del os.environ["QIBO_GB300_DF_FP64_WARPS"]
         assert np.max(np.abs(np.asarray(st) - want)) < 1e-12, w
+
+
+def test_backend_apply_gate_c128(backend):
+    """Backend.apply_gate (the reference's per-gate entry point,
+    backends/abstract.py:2322-2361) in complex128: dense 1- and 2-qubit gates
+    in the FP64 / double-float warp mix by default, IEEE FP64 with
+    strict_fp64; other gates through their own kernels.  Against the FP64
+    oracle to 1e-12."""
+    from qibo_gb300 import gates
+    from qibo_gb300.device import DeviceState
+
+    n = 12
+    psi = rand_state(n, 91)
+    ops = [("U3", (0,), (0.3, 1.1, -0.4)), ("H", (n - 1,), ()), ("RY", (3,), (0.7,)), ("CNOT", (2, 9), ()),
+           ("fSim", (5, 1), (0.4, 0.9)), ("CZ", (4, 7), ()), ("TOFFOLI", (0, 6, 11), ()), ("SWAP", (8, 10), ()),
+           ("U3", (n - 2,), (1.3, -0.2, 0.6)), ("CU3", (6, 3), (0.5, 0.1, -0.8))]
+    want = ref.execute(ops, n, psi)
+    for strict in (False, True):
+        backend.strict_fp64 = strict
+        try:
+            st = DeviceState.from_numpy(psi)
+            for name, qs, params in ops:
+                st = backend.apply_gate(getattr(gates, name)(*qs, *params), st, n)
+            got = np.asarray(st)
+        finally:
+            backend.strict_fp64 = False
+        assert np.max(np.abs(got - want)) < TOL128, strict
