@@ -303,7 +303,7 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
     norm_f = b64.engine_gb.renormalize(st64)
     inf_f = infidelity()
     # the tensor-core kernel alone: 10 launches of the first 5-qubit block
-    tc_gbs = None
+    tc_gbs = tc_kernel = None
     blk = next((d for d in fdescs if len(d[0]) == 5 and not d[1]), None)
     if blk is not None:
         from qibo_gb300 import _lib
@@ -317,6 +317,8 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
             check(lib.qgb_apply_fused5_tc(st64.ptr, n, st64.code, qs, mp, rt.stream))
         tc_ms = ev.stop_ms(rt.stream) / 10
         tc_gbs = 2 * 2**n * 8 / (tc_ms * 1e-3) / 1e9
+        low = [n - 1 - q for q in blk[0] if n - 1 - q < 4]  # the launcher's placement rule (tcm_fits)
+        tc_kernel = "k_fused5_tcm" if len(low) <= 2 and not {0, 1} <= set(low) else "k_fused5_tc"
     tc_timeout = C.c_int(0)
     check(lib.qgb_tc_status(C.byref(tc_timeout)))
     # plain complex128 per-gate path: IEEE FP64, one kernel per gate (state
@@ -356,6 +358,7 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
                          "circuits_per_s": 1e3 / p50, "infidelity_vs_c128": inf_f,
                          "norm_before_renormalisation": norm_f, "tc_wait_timeouts": tc_timeout.value,
                          "k_fused5_tc_gbs": tc_gbs, "k_fused5_tc_bytes_per_launch": 2 * 2**n * 8,
+                         "k_fused5_tc_note": f"first 5-qubit block of the circuit, 10 launches ({tc_kernel})",
                          "p99_note": "p99 of 8 runs is the slowest run"},
             "c128_per_gate_ms": ms_g, "c128_unfused_passes_ms": ms_128b,
             "c128_per_gate_double_float": {
