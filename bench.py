@@ -317,8 +317,7 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
             check(lib.qgb_apply_fused5_tc(st64.ptr, n, st64.code, qs, mp, rt.stream))
         tc_ms = ev.stop_ms(rt.stream) / 10
         tc_gbs = 2 * 2**n * 8 / (tc_ms * 1e-3) / 1e9
-        low = [n - 1 - q for q in blk[0] if n - 1 - q < 4]  # the launcher's placement rule (tcm_fits)
-        tc_kernel = "k_fused5_tcm" if len(low) <= 2 and not {0, 1} <= set(low) else "k_fused5_tc"
+        tc_kernel = tc64_kernel(n, blk[0])
     tc_timeout = C.c_int(0)
     check(lib.qgb_tc_status(C.byref(tc_timeout)))
     # plain complex128 per-gate path: IEEE FP64, one kernel per gate (state
@@ -624,6 +623,22 @@ def run_serving(args):
                       **serving_sample(args.serving_requests, args.serving_rates)}))
 
 
+def tc64_kernel(n, qubits):
+    """The complex64 block kernel and lane layout the launcher picks for a
+    block on ``qubits`` (tcm_plan in qgb_tc.cu)."""
+    if n < 12:
+        return "k_fused5_tc"
+    bits = sorted(n - 1 - q for q in qubits)
+    low4 = sum(b < 4 for b in bits)
+    strided = 0.45 if {0, 1} <= set(bits) or low4 > 2 else (0.945, 0.94, 0.84)[low4]
+    grp = [b for b in range(n) if b not in bits][:5]
+    k = sum(b in bits[:4] for b in sorted(grp + bits[:4])[:5])
+    shfl = 0.955 if k <= 1 else 0.895 if k == 2 else 0.78 if k == 3 else 0.72
+    if max(strided, shfl) <= 0.74:
+        return "k_fused5_tc"
+    return "k_fused5_tcm (coalesced lanes)" if shfl > strided else "k_fused5_tcm (strided lanes)"
+
+
 def run_tc5(args):
     """The tensor-core block kernels alone: a random 5-qubit unitary applied to
     a state of ``--nqubits`` qubits (default 30; 8.6 GB in complex64, 17.2 GB
@@ -671,14 +686,14 @@ def run_tc5(args):
             ms = ev.stop_ms(rt.stream) / args.steps
             gbs = nbytes / (ms * 1e-3) / 1e9
             kname = kernel
-            low = [n - 1 - q for q in qs if n - 1 - q < 4]
-            if dtype == "complex64" and n >= 12 and len(low) <= 2 and not {0, 1} <= set(low):
-                kname = "k_fused5_tcm"  # A in tensor memory
+            if dtype == "complex64":
+                kname = tc64_kernel(n, qs)
             res[name] = {"qubits": qs, "kernel": kname, "ms": ms, "GB/s": gbs, "frac_of_measured_hbm": gbs / peak,
                          "tensor_tflops": flops * 2 ** (n - 5) / (ms * 1e-3) / 1e12}
         if dtype == "complex64" and n >= 12:
             # both complex64 kernels on placements with 0-5 block qubits on
-            # index bits 0..4 (QIBO_GB300_TC64_KERNEL picks the kernel)
+            # index bits 0..4, k_fused5_tcm with strided and with coalesced
+            # lanes (QIBO_GB300_TC64_KERNEL picks the kernel and layout)
             sweep = []
             for bits in ([5, 10, 15, 20, 25], [0, 10, 15, 20, 25], [4, 10, 15, 20, 25], [3, 4, 12, 18, 24],
                          [0, 2, 12, 18, 24], [2, 3, 4, 15, 25], [0, 2, 4, 15, 25], [0, 1, 12, 18, 24],
@@ -686,7 +701,8 @@ def run_tc5(args):
                 bits = [min(x, n - 5 + i) if x >= 5 else x for i, x in enumerate(bits)]
                 qa = _lib.int_array([n - 1 - x for x in bits])
                 row = {"index_bits": bits}
-                for kname, pick in (("k_fused5_tcm", "tmem"), ("k_fused5_tc", "smem")):
+                for kname, pick in (("k_fused5_tcm", "tmem-strided"), ("k_fused5_tcm_coalesced", "tmem-shfl"),
+                                    ("k_fused5_tc", "smem")):
                     os.environ["QIBO_GB300_TC64_KERNEL"] = pick
                     try:
                         for _ in range(args.warmup):

@@ -34,7 +34,7 @@
 //
 // On full tiles most placements run k_fused5_tcm instead (below): A goes to
 // tensor memory from registers, with no shared-memory staging, which takes
-// a block from 0.69-0.74 to 0.83-0.96 of HBM bandwidth.
+// a block from 0.69-0.74 to 0.79-0.96 of HBM bandwidth.
 //
 // The wait on the mbarrier is bounded: on timeout the kernel records an
 // error flag, waits once more (bounded) for the in-flight MMAs, frees its
@@ -269,12 +269,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 }
 
 // The same product with A in tensor memory (states of 12 qubits or more,
-// blocks that tcm_fits accepts).  A warp's lanes are 32 consecutive group
-// rows; for a block with no qubit on index bits 0..4 those are index bits
-// 0..4, and every warp access is 256 contiguous bytes; with block qubits
-// there the lanes are strided and L1/L2 merge the sectors of a row's
-// columns, which costs little while a warp access spans at most 8 lines.
-// Each thread loads
+// placements tcm_plan selects).  After the load, thread l of warp w holds
+// group row 32 (w % 4) + l.  Two lane layouts get it there: strided lanes
+// (the lanes are group rows; a warp access spans 2^(1 + b) lines, b = block
+// qubits on index bits 0..3, and L1/L2 merge the sectors of a row's
+// columns), or coalesced lanes (every warp access is one or two 128-byte
+// lines, and up to four warp-shuffle exchanges of lane and register bits
+// move rows onto lanes).  Each thread loads
 // the 16 amplitudes of its row in one column half straight into registers,
 // splits them and writes A_hi / A_lo to its own tensor-memory lane with
 // tcgen05.st; the MMAs read A from tensor memory and only B from shared
@@ -287,17 +288,51 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 #define TCM_SMEM (2 * TC_B_BYTES)
 
 // Tile geometry: a tile is the 5 block bits plus the 7 lowest other index
-// bits.  Thread (warp w, lane l) holds group row 32 (w % 4) + l and block
-// columns 16 h .. 16 h + 15, h = w / 4; its amplitude j sits at
-// base(tile) + lanes[l] + rowhi[w % 4] + h * chi + clo[j].
+// bits.  Thread (warp w, lane l) loads and stores amplitude r at
+// base(tile) + lanes[l] + rowhi[w % 4] + h * chi + clo[r], h = w / 4.
+// With nswap = 0 (strided lanes) lanes[] are the group-row bits and clo[]
+// the block columns, so thread l holds group row 32 (w % 4) + l, columns
+// 16 h + r.  With nswap = k > 0 (coalesced lanes) lane bits 0..k-1 address
+// block bits and register bits 0..k-1 group-row bits; exchanging lane bit i
+// with register bit i (i < k, warp shuffles) after the load, and again
+// before the store, gives the same row / column layout.
 struct TcmGeom {
   int nrest;
   int rest[32];
-  i64 lanes[32];  // offsets of group-row bits 0..4
+  int nswap;      // lane bits exchanged with register bits (0-4)
+  i64 lanes[32];  // offsets of the lane bits
   i64 rowhi[4];   // offsets of group-row bits 5, 6
-  i64 chi;       // offset of block column bit 4
-  i64 clo[16];   // offsets of block columns 0..15
+  i64 chi;        // offset of block column bit 4
+  i64 clo[16];    // offsets of the register bits
 };
+
+// Exchange lane bit I with register bit I of v: the value held for (lane
+// bit a, register bit b) moves to (lane bit b, register bit a).  All lanes
+// of the warp take part.
+template <int I>
+__device__ __forceinline__ void tcm_swap(float2 (&v)[16], int lane) {
+  const bool up = (lane >> I) & 1;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    if (r & (1 << I)) continue;
+    const int r1 = r | (1 << I);
+    const float2 send = up ? v[r] : v[r1];
+    float2 recv;
+    recv.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << I);
+    recv.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << I);
+    if (up) v[r] = recv;
+    else v[r1] = recv;
+  }
+}
+
+// the exchanges commute and each is its own inverse: the same call maps
+// the load layout to rows and the rows back to the store layout
+__device__ __forceinline__ void tcm_transpose(float2 (&v)[16], int lane, int nswap) {
+  if (nswap > 0) tcm_swap<0>(v, lane);
+  if (nswap > 1) tcm_swap<1>(v, lane);
+  if (nswap > 2) tcm_swap<2>(v, lane);
+  if (nswap > 3) tcm_swap<3>(v, lane);
+}
 
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_fused5_tcm(float2* __restrict__ psi, i64 ntiles, const __grid_constant__ TcmGeom geo,
@@ -354,6 +389,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   }
   for (; t < ntiles; t += gridDim.x) {
     // registers -> A_hi, A_lo (columns 2c, 2c + 1 = re, im of element c)
+    tcm_transpose(v, lane, geo.nswap);
     {
       float a[32];
 #pragma unroll
@@ -419,9 +455,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     tmem_ld16(tlane, y);
     tmem_ld16(tlane + 16, y + 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    float2* dst = psi + base + toff;
+    {
+      float2 o[16];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) dst[geo.clo[j]] = make_float2(y[2 * j], y[2 * j + 1]);
+      for (int j = 0; j < 16; ++j) o[j] = make_float2(y[2 * j], y[2 * j + 1]);
+      tcm_transpose(o, lane, geo.nswap);
+      float2* dst = psi + base + toff;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) dst[geo.clo[j]] = o[j];
+    }
     // D and A are rewritten next: every thread's tensor-memory reads are done
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -528,40 +570,88 @@ void block_perm(const int cbit[5], int idx[32]) {
   }
 }
 
-// Geometry of k_fused5_tcm for target bits tbits in a state of 12 qubits
-// or more.  Block column bit i is the i-th lowest target, as in make_geom,
-// so block_perm of make_geom's cbit applies.
-void make_geom_m(int n, const std::vector<int>& tbits, TcmGeom* geo) {
-  std::vector<int> sorted_t = tbits;
-  std::sort(sorted_t.begin(), sorted_t.end());
+// Geometry of k_fused5_tcm for target bits tbits (index positions, matrix
+// order) in a state of 12 qubits or more, and the column bit cbit[jt] of
+// each target for block_perm.  Strided (shfl false): lanes are group rows
+// 0..4, registers block columns 0..3, column bit i the i-th lowest target.
+// Coalesced (shfl true): P = group-row bits 0..4 and the 4 lowest targets;
+// lanes take the 5 lowest positions of P (index bits 0..4, or 0..3 and 5
+// when the block is index bits 0..4), registers the other 4.  The k block
+// bits among the lanes go first (lane bits 0..k-1), as do the k row bits
+// among the registers, so exchanging lane and register bits 0..k-1 leaves
+// rows on the lanes and block columns on the registers; block column bits
+// 0..3 are then the exchanged block bits followed by the register ones.
+void make_geom_m(int n, const std::vector<int>& tbits, bool shfl, TcmGeom* geo, int cbit[5]) {
+  std::vector<int> st = tbits;
+  std::sort(st.begin(), st.end());
   std::vector<int> grp;
   for (int b = 0; b < n && (int)grp.size() < 7; ++b)
     if (std::find(tbits.begin(), tbits.end(), b) == tbits.end()) grp.push_back(b);
+  std::vector<int> lpos, rpos, colpos;
+  if (!shfl) {
+    lpos.assign(grp.begin(), grp.begin() + 5);
+    rpos.assign(st.begin(), st.begin() + 4);
+    colpos = rpos;
+    geo->nswap = 0;
+  } else {
+    std::vector<int> P(grp.begin(), grp.begin() + 5);
+    P.insert(P.end(), st.begin(), st.begin() + 4);
+    std::sort(P.begin(), P.end());
+    const std::vector<int> low5(P.begin(), P.begin() + 5), up4(P.begin() + 5, P.end());
+    auto in = [](const std::vector<int>& v, int x) { return std::find(v.begin(), v.end(), x) != v.end(); };
+    std::vector<int> blow, lrow, rup, ucol;
+    for (int b : low5) (in(grp, b) ? lrow : blow).push_back(b);
+    for (int b : up4) (in(grp, b) ? rup : ucol).push_back(b);
+    lpos = blow;
+    lpos.insert(lpos.end(), lrow.begin(), lrow.end());
+    rpos = rup;
+    rpos.insert(rpos.end(), ucol.begin(), ucol.end());
+    colpos = blow;
+    colpos.insert(colpos.end(), ucol.begin(), ucol.end());
+    geo->nswap = (int)blow.size();
+  }
+  colpos.push_back(st[4]);
+  for (int jt = 0; jt < 5; ++jt)
+    cbit[jt] = (int)(std::find(colpos.begin(), colpos.end(), tbits[jt]) - colpos.begin());
   for (int l = 0; l < 32; ++l) {
     geo->lanes[l] = 0;
     for (int i = 0; i < 5; ++i)
-      if ((l >> i) & 1) geo->lanes[l] += (i64)1 << grp[i];
+      if ((l >> i) & 1) geo->lanes[l] += (i64)1 << lpos[i];
   }
   for (int k = 0; k < 4; ++k)
     geo->rowhi[k] = ((k & 1) ? (i64)1 << grp[5] : 0) + ((k & 2) ? (i64)1 << grp[6] : 0);
-  for (int j = 0; j < 16; ++j) {
-    geo->clo[j] = 0;
+  for (int r = 0; r < 16; ++r) {
+    geo->clo[r] = 0;
     for (int i = 0; i < 4; ++i)
-      if ((j >> i) & 1) geo->clo[j] += (i64)1 << sorted_t[i];
+      if ((r >> i) & 1) geo->clo[r] += (i64)1 << rpos[i];
   }
-  geo->chi = (i64)1 << sorted_t[4];
+  geo->chi = (i64)1 << st[4];
   geo->nrest = 0;
   for (int b = 0; b < n; ++b)
     if (std::find(tbits.begin(), tbits.end(), b) == tbits.end() && std::find(grp.begin(), grp.end(), b) == grp.end())
       geo->rest[geo->nrest++] = b;
 }
 
-// k_fused5_tcm's warp accesses touch 2^(5 - u) 128-byte lines, u = index
-// bits 0..3 that are not block bits, and up to 32 sectors when index bits
-// 0 and 1 are both block bits.  Measured at n=30 (8.6 GB, 12 placements):
-// with at most 8 lines and 16 sectors it moves 0.83-0.96 of HBM bandwidth,
-// with more 0.31-0.57, against 0.69-0.74 for k_fused5_tc on every placement.
-bool tcm_fits(const std::vector<int>& tbits) {
+// The kernel and lane layout a full-tile block runs with: the larger of
+// two estimates, each the fraction of HBM bandwidth measured at n=30 (8.6
+// GB, 12 placements, `bench.py --workload tc5`), against 0.74 for
+// k_fused5_tc.  Strided lanes, by 128-byte lines per warp access (2: 0.945,
+// 4: 0.94, 8: 0.84; 32 sectors, when index bits 0 and 1 are both block
+// bits, or more lines: 0.31-0.55).  Coalesced lanes, by lane / register
+// exchanges (0-1: 0.955, 2: 0.895, 3: 0.78, 4: 0.72).
+enum { TCM_OFF = 0, TCM_STRIDED = 1, TCM_SHFL = 2 };
+int tcm_swaps(const std::vector<int>& tbits) {  // the nswap of make_geom_m's coalesced layout
+  std::vector<int> st = tbits, P;
+  std::sort(st.begin(), st.end());
+  for (int b = 0; (int)P.size() < 5; ++b)
+    if (std::find(tbits.begin(), tbits.end(), b) == tbits.end()) P.push_back(b);
+  P.insert(P.end(), st.begin(), st.begin() + 4);
+  std::sort(P.begin(), P.end());
+  int k = 0;
+  for (int i = 0; i < 5; ++i) k += std::find(st.begin(), st.begin() + 4, P[i]) != st.begin() + 4;
+  return k;
+}
+int tcm_plan(const std::vector<int>& tbits) {
   int low4 = 0;
   bool b0 = false, b1 = false;
   for (int b : tbits) {
@@ -569,7 +659,11 @@ bool tcm_fits(const std::vector<int>& tbits) {
     b0 |= b == 0;
     b1 |= b == 1;
   }
-  return low4 <= 2 && !(b0 && b1);
+  const double strided = (b0 && b1) || low4 > 2 ? 0.45 : low4 == 0 ? 0.945 : low4 == 1 ? 0.94 : 0.84;
+  const int k = tcm_swaps(tbits);
+  const double shfl = k <= 1 ? 0.955 : k == 2 ? 0.895 : k == 3 ? 0.78 : 0.72;
+  if (std::max(strided, shfl) <= 0.74) return TCM_OFF;
+  return shfl > strided ? TCM_SHFL : TCM_STRIDED;
 }
 
 template <bool FULL>
@@ -592,6 +686,20 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   TcGeom* geo = new TcGeom();
   int cbit[5];
   make_geom(n, g.tbits, geo, cbit);
+  const i64 ntiles = (i64)1 << (n - geo->nbits);
+  const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
+  // QIBO_GB300_TC64_KERNEL=smem / tmem-strided / tmem-shfl picks the kernel
+  // on full tiles (for comparisons); otherwise tcm_plan decides
+  const char* pick = getenv("QIBO_GB300_TC64_KERNEL");
+  const int plan = pick && !strcmp(pick, "smem")           ? TCM_OFF
+                   : pick && !strcmp(pick, "tmem-strided") ? TCM_STRIDED
+                   : pick && !strcmp(pick, "tmem-shfl")    ? TCM_SHFL
+                                                           : tcm_plan(g.tbits);
+  TcmGeom* gm = nullptr;
+  if (geo->nbits == 12 && plan != TCM_OFF) {
+    gm = new TcmGeom();
+    make_geom_m(n, g.tbits, plan == TCM_SHFL, gm, cbit);
+  }
   int idx[32];
   block_perm(cbit, idx);
   TcGate* G = new TcGate();
@@ -601,17 +709,7 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
       G->ur[r][c] = (float)u.real();
       G->ui[r][c] = (float)u.imag();
     }
-  const i64 ntiles = (i64)1 << (n - geo->nbits);
-  const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms() * 2);
-  // QIBO_GB300_TC64_KERNEL=smem / tmem picks the kernel on full tiles
-  // (for comparisons); unset or anything else, tcm_fits decides
-  const char* pick = getenv("QIBO_GB300_TC64_KERNEL");
-  const bool use_tcm = pick && !strcmp(pick, "smem")   ? false
-                       : pick && !strcmp(pick, "tmem") ? true
-                                                       : tcm_fits(g.tbits);
-  if (geo->nbits == 12 && use_tcm) {
-    TcmGeom* gm = new TcmGeom();
-    make_geom_m(n, g.tbits, gm);
+  if (gm) {
     k_fused5_tcm<<<blocks, TC_THREADS, TCM_SMEM, s>>>((float2*)state, ntiles, *gm, *G, err);
     delete gm;
   } else if (geo->nbits == 12) {

@@ -61,6 +61,31 @@ def test_fused5_tc_matches_oracle(n, qubits):
     assert np.max(np.abs(got - want)) < 2e-6
 
 
+@pytest.mark.parametrize("mode", ["smem", "tmem-strided", "tmem-shfl"])
+def test_fused5_tc_every_kernel_every_placement(mode):
+    """Full tiles in each complex64 block kernel and lane layout
+    (QIBO_GB300_TC64_KERNEL), on placements with 0-5 block qubits on index
+    bits 0..4, against the FP64 oracle."""
+    import os
+
+    placements = [(12, (0, 1, 2, 3, 4)), (12, (11, 10, 9, 8, 7)), (13, (12, 4, 9, 1, 6)), (14, (13, 12, 5, 2, 0)),
+                  (14, (9, 10, 11, 12, 13)), (15, (14, 12, 7, 3, 0)), (16, (15, 14, 13, 12, 4)),
+                  (16, (1, 15, 8, 4, 12)), (17, (16, 15, 14, 13, 2)), (18, (14, 13, 2, 9, 5))]
+    os.environ["QIBO_GB300_TC64_KERNEL"] = mode
+    try:
+        for n, qubits in placements:
+            rng = np.random.default_rng(n + sum(qubits))
+            psi = rng.normal(size=2**n) + 1j * rng.normal(size=2**n)
+            psi /= np.linalg.norm(psi)
+            psi = psi.astype(np.complex64).astype(np.complex128)
+            u = _unitary(n + 3)
+            got = _apply_tc(psi, qubits, u)
+            want = ref.apply_gate(psi, u, list(qubits), n)
+            assert np.max(np.abs(got - want)) < 2e-6, (mode, n, qubits)
+    finally:
+        del os.environ["QIBO_GB300_TC64_KERNEL"]
+
+
 def test_fused5_tc_block_of_a_brickwork():
     """A real fused block (U3 + CZ gates packed by the fusion pass)."""
     from qibo_gb300 import Circuit, gates
