@@ -15,6 +15,7 @@
 // The tensor-memory variant k_fused5_tcm is replayed the same way with the
 // tables of make_geom_m.  No kernel is launched.
 #include <complex>
+#include <cstring>
 #include <cstdio>
 #include <map>
 #include <random>
@@ -217,7 +218,17 @@ static int check_tcm(std::mt19937_64& rng) {
   return fails;
 }
 
-int main() {
+int main(int argc, char** argv) {
+  if (argc > 1 && !strcmp(argv[1], "plans")) {  // tcm_plan of every 5-bit block of a 16-qubit state
+    for (int m = 0; m < (1 << 16); ++m) {
+      if (__builtin_popcount(m) != 5) continue;
+      std::vector<int> tb;
+      for (int b = 0; b < 16; ++b)
+        if ((m >> b) & 1) tb.push_back(b);
+      printf("%d,%d,%d,%d,%d %d\n", tb[0], tb[1], tb[2], tb[3], tb[4], tcm_plan(tb));
+    }
+    return 0;
+  }
   std::mt19937_64 rng(5);
   std::normal_distribution<double> nd;
   int fails = 0, cases = 0, bank_fails = 0;

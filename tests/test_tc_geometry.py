@@ -48,6 +48,31 @@ def test_tc_geometry_tables(tmp_path):
     assert "index failures 0 bank-pattern failures 0" in out
 
 
+def test_bench_labels_follow_the_launcher_plan(tmp_path):
+    """bench.py names the complex64 block kernel a placement runs on with a
+    copy of the launcher's tcm_plan; both agree on every 5-qubit block of a
+    16-qubit state."""
+    import importlib.util
+
+    _build_and_run(tmp_path, "tc_geometry_check")
+    r = subprocess.run([str(tmp_path / "tc_geometry_check"), "plans"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    names = {0: "k_fused5_tc", 1: "k_fused5_tcm (strided lanes)", 2: "k_fused5_tcm (coalesced lanes)"}
+    lines = r.stdout.split("\n")
+    checked = 0
+    for line in lines:
+        if not line.strip():
+            continue
+        bits, plan = line.split()
+        bits = [int(x) for x in bits.split(",")]
+        assert bench.tc64_kernel(16, [15 - b for b in bits]) == names[int(plan)], bits
+        checked += 1
+    assert checked == 4368
+
+
 def test_oz_complex128_blocks(tmp_path):
     out = _build_and_run(tmp_path, "oz_check")
     assert "index failures 0 exactness failures 0 bank-pattern failures 0" in out
