@@ -35,7 +35,8 @@ int qgb_classify(int nqubits, const int* qubits, int k, const int* controls, int
 // dense blocks.  complex64 3xTF32; complex128 Ozaki scheme (n >= 12), on
 // IEEE doubles or, inside a chain, on the fixed-point format.
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);
-int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix);
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix,
+                         uint32_t* fix_words = nullptr, int b = 0);
 bool qgb_oz_unitary(const GateOp& g);
 int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);
 int qgb_tc_prepare();  // allocate the tensor-core paths' device buffers (idempotent)

@@ -9,40 +9,62 @@
 // multiplication and its applications", Numer. Algorithms 59 (2012)):
 //
 //  * every value of a tile (and every entry of a gate row) is written in
-//    47-bit fixed point against the largest exponent sharing its scale (one
-//    per tile of A, one per output row of B), and split into six balanced
-//    base-256 digits d in [-128, 128] (exact as bf16);
+//    47-bit fixed point against a shared scale (IEEE doubles: the largest
+//    exponent of the tile; the fixed-point chain format: one shift for the
+//    whole launch, from the OR of the state's magnitudes; gate rows: their
+//    largest entry, or the block's in the chain format) and split into six
+//    balanced base-256 digits d in [-128, 128] (exact as bf16);
 //  * A_i * B_j^T over K = 64 then sums products of at most 2^14, so every
 //    level l = i + j <= 6 accumulates exactly in its own FP32 accumulator
 //    (|sum| <= 7 * 2^20 < 2^24);
 //  * the seven level accumulators are combined with integer arithmetic into
 //    sum_{l<=5} acc_l 256^(5-l) + round(acc_6 / 256) and rounded once to an
-//    IEEE double.
-//  With 2^E, 2^F the tile and gate-row scales (2^E <= 2 x the tile's largest
-//  |value|), the fixed-point rounding of both operands over K = 64 and the
-//  dropped levels (l >= 7) bound the error of an output by 2^(E + F - 41);
-//  independent roundings give about 2^(E + F - 46).  Normalised states and
-//  unitary blocks have 2^(E + F) <= 4, and far less for spread-out states.
-//  The CPU replay tests/native/oz_check.cu checks the bound output by output.
+//    IEEE double (the chain format keeps the lowest three levels to within
+//    645 units of that sum, see oz_combine_fix).
+//  With 2^E, 2^F the A and B scales (2^E <= 2 x the largest |value|
+//  sharing it), the fixed-point rounding of both operands over K = 64 and
+//  the dropped levels (l >= 7) bound the error of an output by
+//  2^(E + F - 41); independent roundings give about 2^(E + F - 46).
+//  Normalised states and unitary blocks have 2^(E + F) <= 4, and far less
+//  for spread-out states.  The CPU replay tests/native/oz_check.cu checks
+//  the bound output by output.
 //
-// Tensor memory holds the seven level accumulators side by side (columns
-// 64 l .. 64 l + 63, 448 of 512).  The six B slices are stacked along N (rows
-// 64 j + n), so the MMA for A slice i with B slices 0..min(5, 6-i) written at
-// TMEM column 64 i lands each product A_i B_j in level i + j: 9 instructions
-// per K-step of 16 (N = 384 and 320 are split at 256; the first write of
-// level 6 is its own instruction so that it starts the accumulation), 37
-// per tile.
+// Tensor memory holds the level accumulators of the two output halves
+// (realified output rows 0-31 and 32-63) in two rings of seven levels:
+// level l of half h at columns 256 h + 32 l .. + 31 (224 columns per half).
+// The six B slices are stacked per half along N (row 192 h + 32 j + n'), so
+// the MMA for A slice i with B slices 0..min(5, 6-i) written at TMEM column
+// 256 h + 32 i lands each product A_i B_j in level i + j: one instruction
+// per slice and K-step of 16 (N = 32 x slices <= 192; the first write of
+// level 6 is its own instruction so that it starts the accumulation), 25
+// per half and tile.
 //
-// A CTA (512 threads, one per SM: 223 KB of shared memory, 448 TMEM columns)
-// owns 4096-amplitude tiles with the index geometry of qgb_tc.cu.  Warps 0-7
-// convert (thread t moves amplitudes t + 256 r, r < 16, prefetched into
-// registers while the previous MMAs run) and issue the MMAs; warps 8-15 read
-// the levels from TMEM, combine and store, overlapping the conversion of the
-// next tile.  The digit split runs on the FMA pipe (exact FP32 arithmetic
-// on 16-bit chunks), the level combination as an integer multiply-add chain.
-// Every wait on an mbarrier is bounded: on timeout the kernel records an
-// error flag, both groups stop at their next check, the converter waits once
-// more (bounded) for its in-flight MMAs, and tensor memory is freed.
+// A CTA (544 threads, one per SM: 224 KB of shared memory, 448 TMEM
+// columns) owns 4096-amplitude tiles with the index geometry of qgb_tc.cu,
+// in three roles that run as a pipeline:
+//  * warps 0-7 convert (thread t moves amplitudes t + 256 r, r < 16).  The
+//    raw tile is copied into shared memory by the bulk-copy engine one tile
+//    ahead (32 runs of 128 contiguous amplitudes), so the loads stay in
+//    flight without holding registers.  A thread reads its amplitudes,
+//    forms their digit words, frees the raw buffer for the next copy, and
+//    writes digit slice s of A as soon as the previous tile's MMAs on slice
+//    s are done;
+//  * warp 16 (one thread) issues the MMAs: half 0 of tile i slice by slice
+//    as the slices are written (once the epilogue has read half 0 of tile
+//    i - 1), then half 1, committing "slice s free" after each of its
+//    slices;
+//  * warps 8-15 read each half's levels from TMEM (lane quarter = warp mod
+//    4, 16 of the half's 32 output reals per warp), combine and store;
+//    half 0 overlaps the MMAs of half 1, half 1 those of the next tile's
+//    half 0.
+// The digits are bytes: with Z = X + 0x8080808080 (X the 47-bit value),
+// byte k of Z minus 128 is the digit of weight 256^k (k < 5) and Z >> 40
+// the top one; a byte permutation puts each byte under the exponent of 2^23
+// and one FP32 subtraction makes it an exact float.  The level combination
+// is an integer multiply-add chain.  Every wait on an mbarrier is bounded
+// and also ends when another role has recorded an abort; the MMA thread
+// then waits once more (bounded) for its in-flight MMAs, the converters for
+// an in-flight copy, and tensor memory is freed.
 //
 // Runs of unitary blocks (qgb_run_oz_chain) keep the state in a 64-bit
 // fixed-point format between blocks (k_fused5_oz<true>), converted from and
@@ -57,29 +79,44 @@
 #include "qgb_plan.h"
 #include "qgb_tcgen05.cuh"
 
-#define OZ_THREADS 512  // 8 converter warps + 8 epilogue warps
-#define OZ_GROUP 256    // threads per group
-#define OZ_STEPS 16     // amplitudes per group thread per tile
-#define OZ_TILE 4096   // amplitudes per tile
-#define OZ_NSLICE 6    // digits per value
-#define OZ_NLEVEL 7    // digit-product levels kept (i + j <= 6)
+#define OZ_CONV_WARPS 8                        // converter warps 0-7
+#define OZ_EPI_WARPS 8                         // epilogue warps 8-15 (lane quarter = warp mod 4)
+#define OZ_MMA_WARP (OZ_CONV_WARPS + OZ_EPI_WARPS)  // warp 16: MMA issue
+#define OZ_THREADS ((OZ_MMA_WARP + 1) * 32)    // 544
+#define OZ_GROUP (OZ_CONV_WARPS * 32)          // converter threads
+#define OZ_EPI (OZ_EPI_WARPS * 32)             // epilogue threads
+#define OZ_STEPS 16     // amplitudes per converter thread per tile
+#define OZ_TILE 4096    // amplitudes per tile
+#define OZ_NSLICE 6     // digits per value
+#define OZ_NLEVEL 7     // digit-product levels kept (i + j <= 6)
 #define OZ_TMEM_COLS 512
+#define OZ_HALF_COLS 256  // TMEM column of output half 1
+#define OZ_C5 0x8080808080ull  // 128 in each of the five low digit bytes
 // A slices: 128 rows x 64 bf16, K-major no-swizzle core matrices (8 rows x
 // 16 B); row groups 144 B apart, K chunks a_lbo = 2304 + 16 rot apart.
 #define OZ_A_SBO 144
 #define OZ_A_LBO0 2304
 #define OZ_A_SLICE (8 * (OZ_A_LBO0 + 64))  // 18944
-// B: 384 rows (6 slices x 64) x 64 bf16, dense core matrices
+// B: 384 rows ([half][slice][32 rows]) x 64 bf16, dense core matrices
 #define OZ_B_ROWS (OZ_NSLICE * 64)
 #define OZ_B_SBO 128
 #define OZ_B_LBO (OZ_B_ROWS / 8 * OZ_B_SBO)  // 6144
+// Raw tile: the 32 runs of 128 contiguous amplitudes of the next tile (2 KB
+// each), copied in by the bulk-copy engine: run 2 r + (g >> 7) holds the
+// amplitudes of converter thread g's step r.
+#define OZ_RUN 2048
+#define OZ_RAW_BYTES (32 * OZ_RUN)  // 65536
 #define OZ_OFF_A 0
 #define OZ_OFF_B (OZ_OFF_A + OZ_NSLICE * OZ_A_SLICE)  // 113664
-#define OZ_SMEM (OZ_OFF_B + 8 * OZ_B_LBO)             // 162816
+#define OZ_OFF_RAW (OZ_OFF_B + 8 * OZ_B_LBO)          // 162816
+#define OZ_SMEM (OZ_OFF_RAW + OZ_RAW_BYTES)           // 228352
 
-static_assert(OZ_OFF_B % 16 == 0, "operand regions 16-byte aligned");
-static_assert(OZ_SMEM <= 227 * 1024, "one CTA per SM");
-static_assert(OZ_GROUP * OZ_STEPS == OZ_TILE, "one amplitude per group thread and step");
+static_assert(OZ_OFF_B % 16 == 0 && OZ_OFF_RAW % 128 == 0, "operand regions aligned");
+static_assert(OZ_SMEM + 1024 <= 232448, "one CTA per SM");
+static_assert(OZ_GROUP * OZ_STEPS == OZ_TILE, "one amplitude per converter thread and step");
+
+// shared-memory offset of A slice s
+__host__ __device__ __forceinline__ uint32_t oz_slot(int s) { return (uint32_t)(s * OZ_A_SLICE); }
 
 // Tile geometry (the tile of the complex64 kernel).  Loads: tile index
 // j = t + 256 r (t a converter thread) has global offset base + (t & 127) +
@@ -153,14 +190,7 @@ __host__ __device__ __forceinline__ int64_t oz_fix47(double x, int exm) {
   return (int32_t)hi < 0 ? -X : X;
 }
 
-// exact float of an integer 0 <= c < 2^23, and of |c| < 2^22
-__host__ __device__ __forceinline__ float oz_u2f(uint32_t c) {
-#ifdef __CUDA_ARCH__
-  return __uint_as_float(0x4B000000u | c) - 8388608.0f;
-#else
-  return (float)c;
-#endif
-}
+// exact float of an integer |c| < 2^22
 __host__ __device__ __forceinline__ float oz_i2f(int32_t c) {
 #ifdef __CUDA_ARCH__
   return __int_as_float(0x4B400000 + c) - 12582912.0f;
@@ -169,38 +199,49 @@ __host__ __device__ __forceinline__ float oz_i2f(int32_t c) {
 #endif
 }
 
-// nearest integer, ties to even, of |v| < 2^22, as a float (IEEE addition:
-// neither compiler folds (v + C) - C without fast-math)
-__host__ __device__ __forceinline__ float oz_rintf(float v) { return (v + 12582912.0f) - 12582912.0f; }
-
-// Balanced base-256 digits of a 47-bit fixed-point value, as exact floats:
-//   X = sum_{i<6} d[i] 256^(5-i),   |d[i]| <= 128.
-// X splits into a signed top (bits 32..47) and two 16-bit chunks, each
-// converted exactly to FP32; every digit is then w - 256 rint(w / 256) on
-// the FMA pipe, carrying rint(.) upwards.
-__host__ __device__ __forceinline__ void oz_digits_f(int64_t X, float d[OZ_NSLICE]) {
-  const uint32_t lo = (uint32_t)X;
-  const int32_t hi = (int32_t)(X >> 32);
-  float w = oz_u2f(lo & 0xFFFFu);
-  float q = oz_rintf(w * 0.00390625f);
-  d[5] = w - 256.0f * q;
-  float t = oz_rintf(q * 0.00390625f);
-  d[4] = q - 256.0f * t;
-  w = oz_u2f(lo >> 16) + t;
-  q = oz_rintf(w * 0.00390625f);
-  d[3] = w - 256.0f * q;
-  t = oz_rintf(q * 0.00390625f);
-  d[2] = q - 256.0f * t;
-  w = oz_i2f(hi) + t;
-  q = oz_rintf(w * 0.00390625f);
-  d[1] = w - 256.0f * q;
-  d[0] = q;
+// byte k (0..3) of w minus 128, as an exact float: the byte is placed under
+// the exponent of 2^23 by one byte permutation and 2^23 + 128 subtracted
+__host__ __device__ __forceinline__ float oz_bytef(uint32_t w, int k) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)) - 8388736.0f;
+#else
+  return (float)(int)((w >> (8 * k)) & 0xFFu) - 128.0f;
+#endif
 }
 
-// the same digits as integers (host checks and the B slices)
+// Balanced base-256 digits of a 47-bit fixed-point value X (|X| <= 2^47),
+// as exact floats, from Z = X + OZ_C5:
+//   X = sum_{i<6} d[i] 256^(5-i),  d[0] = Z >> 40 in [-128, 128],
+//   d[i] = byte 5 - i of Z minus 128 in [-128, 127] (i >= 1),
+// since the five low bytes of OZ_C5 are 128 each.  The top digit: Z lies in
+// [-2^47, 2^47 + 2^40), so Z >> 40 lies in [-128, 128].
+__host__ __device__ __forceinline__ void oz_zdigits_top(uint64_t Z, float d[3]) {
+  const uint32_t hi = (uint32_t)(Z >> 32);
+  d[0] = oz_i2f((int32_t)hi >> 8);
+  d[1] = oz_bytef(hi, 0);
+  d[2] = oz_bytef((uint32_t)Z, 3);
+}
+// digits 3..5 from the low word of Z
+__host__ __device__ __forceinline__ void oz_zdigits_low(uint32_t zlo, float d[3]) {
+  d[0] = oz_bytef(zlo, 2);
+  d[1] = oz_bytef(zlo, 1);
+  d[2] = oz_bytef(zlo, 0);
+}
+__host__ __device__ __forceinline__ void oz_zdigits(uint64_t Z, float d[OZ_NSLICE]) {
+  oz_zdigits_top(Z, d);
+  oz_zdigits_low((uint32_t)Z, d + 3);
+}
+
+// digit s of Z alone (oz_zdigits)
+__host__ __device__ __forceinline__ float oz_zdigit(uint64_t Z, int s) {
+  const uint32_t hi = (uint32_t)(Z >> 32), lo = (uint32_t)Z;
+  return s == 0 ? oz_i2f((int32_t)hi >> 8) : s == 1 ? oz_bytef(hi, 0) : oz_bytef(lo, 5 - s);
+}
+
+// the digits of oz_fix47(x, exm) as integers (host checks and the B slices)
 __host__ __device__ __forceinline__ void oz_digits(double x, int exm, int d[OZ_NSLICE]) {
   float f[OZ_NSLICE];
-  oz_digits_f(oz_fix47(x, exm), f);
+  oz_zdigits((uint64_t)oz_fix47(x, exm) + OZ_C5, f);
 #pragma unroll
   for (int i = 0; i < OZ_NSLICE; ++i) d[i] = (int)f[i];
 }
@@ -274,25 +315,42 @@ __host__ __device__ __forceinline__ double oz_combine(const float acc[OZ_NLEVEL]
   return oz_i64_to_double(oz_levels(acc), sc);
 }
 
-// Shift amounts of round(T 2^k) without branches (one pair per output
-// column, shared by its real and imaginary parts): lsh = max(k, 0),
+// Shift amounts of round(T 2^k) without branches (one set per tile: the
+// fixed-point kernel uses one gate-wide scale F): lsh = max(k, 0),
 // rsh = min(max(-k, 0), 62) (a shift by 62 already rounds every |T| < 2^61
-// to 0).
+// to 0), rnd = 2^rsh / 2.
 struct OzShift {
   int lsh, rsh;
+  int64_t rnd;
 };
 __host__ __device__ __forceinline__ OzShift oz_shift(int k) {
   OzShift r;
   r.lsh = k > 0 ? k : 0;
   r.rsh = k < 0 ? (k > -62 ? -k : 62) : 0;
+  r.rnd = ((int64_t)1 << r.rsh) >> 1;
   return r;
 }
 
-// round(T * 2^k) as a 64-bit integer (fixed-point output; |result| < 2^62),
-// straight-line code
-__host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NLEVEL], OzShift sh) {
-  const int64_t t = (int64_t)((uint64_t)oz_levels(acc) << sh.lsh);
-  return (t + (((int64_t)1 << sh.rsh) >> 1)) >> sh.rsh;
+// round(T' * 2^k) as a 64-bit integer (fixed-point output; |result| < 2^62),
+// where T' = H 2^32 + M 2^16 + Q 2^10 differs from T by the rounding of the
+// three low levels only:
+//   H = acc0 256 + acc1, M = acc2 256 + acc3 (exact: |acc_l| <= 2^22, each
+//   read as an integer by one magic-constant addition; both fit in 31 bits),
+//   Q = round(acc4 / 4 + (acc5 + acc6 / 256) / 1024) in FP32 (two FMA
+//   roundings below 2^-3 and one to an integer: |Q 2^10 - exact| < 580).
+// With the levels dropped (i + j >= 7: below 65) T' is within 645 of the
+// exact product sum in units of T, far inside the digit rounding's 2^13.
+__host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NLEVEL], const OzShift& sh) {
+  const float C = 12582912.0f;
+  const uint32_t K = 0x4B400000u;
+  const uint32_t b0 = oz_fbits(acc[0] + C), b1 = oz_fbits(acc[1] + C);
+  const uint32_t b2 = oz_fbits(acc[2] + C), b3 = oz_fbits(acc[3] + C);
+  const int32_t H = (int32_t)(b0 * 256u + b1 - 257u * K);
+  const int32_t M = (int32_t)(b2 * 256u + b3 - 257u * K);
+  const float s = fmaf(acc[6], 0.00390625f, acc[5]);
+  const int32_t Q = (int32_t)(oz_fbits(fmaf(acc[4], 0.25f, s * 0.0009765625f) + C) - K);
+  const int64_t T = (int64_t)((uint64_t)(uint32_t)H << 32) + (int64_t)M * 65536 + (int64_t)Q * 1024;
+  return ((int64_t)((uint64_t)T << sh.lsh) + sh.rnd) >> sh.rsh;
 }
 
 // Fixed-point state format between consecutive tensor-core blocks: a real
@@ -314,10 +372,14 @@ __host__ __device__ __forceinline__ int64_t oz_to_fix(double x, int e) {
 
 __host__ __device__ __forceinline__ double oz_from_fix(int64_t X, int e) { return oz_i64_to_double(X, e - 62); }
 
-// 47-bit value of a fixed-point X at tile shift sh (the tile's largest |X|
-// is below 2^(47 + sh)), rounding half up
-__host__ __device__ __forceinline__ int64_t oz_fix47_fix(int64_t X, int sh) {
-  return (X + (((int64_t)1 << sh) >> 1)) >> sh;  // sh >= 0; no rounding term for sh = 0
+// Z of the digits (oz_zdigits) of a fixed-point X at tile shift sh (the
+// tile's largest |X| is below 2^(47 + sh)): round(X / 2^sh), half up, plus
+// OZ_C5, as (X + bias) >> sh with bias = oz_fix_bias(sh)
+__host__ __device__ __forceinline__ int64_t oz_fix_bias(int sh) {
+  return (int64_t)((((uint64_t)1 << sh) >> 1) + (OZ_C5 << sh));
+}
+__host__ __device__ __forceinline__ uint64_t oz_fix_z(int64_t X, int sh, int64_t bias) {
+  return (uint64_t)((X + bias) >> sh);
 }
 
 // byte offset of element (row, k) of the stacked B slices (dense, K-major)
@@ -343,35 +405,130 @@ __device__ __forceinline__ void oz_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
 }
 
+// Bounded wait on an mbarrier phase that also gives up once another role
+// has recorded an abort (checked every 64 polls).
+__device__ __forceinline__ bool oz_wait(uint32_t mbar, uint32_t phase, const volatile int* abort_flag) {
+  for (uint32_t it = 0; it < TC_SPIN_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if ((it & 63u) == 63u && *abort_flag) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void oz_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+
+// One 2 KB run of the tile into shared memory by the bulk-copy engine,
+// completing its bytes on mbarrier mbar (the caller set the expected count).
+__device__ __forceinline__ void oz_copy_run(uint32_t dst, const void* src, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"((uint32_t)OZ_RUN), "r"(mbar)
+               : "memory");
+}
+
+// The MMAs of A slices s0..s1-1 for output half h: B slices
+// 0..min(5, 6 - s) of the half land in levels s.. at TMEM column 256 h + 32 s.
+__device__ __forceinline__ void oz_issue(uint32_t s_base, uint32_t tmem, uint32_t a_lbo, int h, int s0, int s1) {
+#pragma unroll 1
+  for (int s = s0; s < s1; ++s) {
+    const int cnt = s <= 1 ? OZ_NSLICE : OZ_NLEVEL - s;  // B slices used with A slice s
+    const uint32_t a0 = s_base + OZ_OFF_A + oz_slot(s);
+    const uint32_t d = tmem + OZ_HALF_COLS * h + 32 * s;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {  // K-steps of 16
+      const uint64_t adesc = smem_desc(a0 + k * 2 * a_lbo, a_lbo, OZ_A_SBO);
+      const uint32_t bs = s_base + OZ_OFF_B + k * 2 * OZ_B_LBO + 24 * h * OZ_B_SBO;  // B row 192 h
+      const uint64_t bdesc = smem_desc(bs, OZ_B_LBO, OZ_B_SBO);
+      if (k == 0 && s == 1) {
+        // levels 1..5 accumulate onto slice 0's products; level 6 starts here
+        oz_mma(d, adesc, bdesc, oz_idesc(160), 1u);
+        oz_mma(d + 160, adesc, smem_desc(bs + 20 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO), oz_idesc(32), 0u);
+      } else {
+        oz_mma(d, adesc, bdesc, oz_idesc(32 * cnt), (s > 0 || k > 0) ? 1u : 0u);
+      }
+    }
+  }
+}
+
+// The epilogue's work on output half H of a tile for a warp of column
+// group CG (reals 16 CG .. 16 CG + 15 of the half, i.e. outputs
+// c = 16 H + 8 CG .. + 7): the seven levels of 8 reals (4 outputs) at a
+// time from TMEM, combined and stored straight to the state; orm collects
+// the OR of the fixed-point outputs' |high words|.
+template <bool FIX, int H, int CG>
+__device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const OzGeom& geo, const OzGate& G,
+                                            const OzShift& fsh, int scale, uint32_t& orm) {
+  const uint32_t th = trow + OZ_HALF_COLS * H;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int c4 = 2 * CG + q;
+    float acc[OZ_NLEVEL][8];
+#pragma unroll
+    for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(th + 32 * l + 8 * c4, acc[l]);
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      const int c = 16 * H + 4 * c4 + (e >> 1);  // output amplitude (permuted block index)
+      float are[OZ_NLEVEL], aim[OZ_NLEVEL];
+#pragma unroll
+      for (int l = 0; l < OZ_NLEVEL; ++l) {
+        are[l] = acc[l][e];
+        aim[l] = acc[l][e + 1];
+      }
+      if (FIX) {
+        const int64_t xr = oz_combine_fix(are, fsh), xi = oz_combine_fix(aim, fsh);
+        orm |= (uint32_t)abs((int32_t)((uint64_t)xr >> 32)) | (uint32_t)abs((int32_t)((uint64_t)xi >> 32));
+        dst[geo.coloff[c]] = make_double2(oz_bitsd((uint64_t)xr), oz_bitsd((uint64_t)xi));
+      } else {
+        const int sc = scale + G.fexp[c] - 2098;
+        dst[geo.coloff[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+      }
+    }
+  }
+}
+
 // FIX: the state holds fixed-point integers (oz_to_fix) instead of IEEE
-// doubles; the tile scale is then a shift and the output a rounding shift.
+// doubles; the launch's scale is then one shift for all tiles, and each
+// output a rounding shift.
 //
-// Warps 0-7 convert: tile scale, digits into the A slices, and thread 0
-// issues the tile's MMAs.  Warps 8-15 read the level accumulators from
-// TMEM, combine them and store them straight to the state.  The converters of tile
-// i + 1 run while the epilogue of tile i runs, and the epilogue's stores
-// overlap the MMAs of tile i + 1.  Handoffs (each completes once per tile,
-// and no waiter can fall two phases behind):
-//   mb_full  (tcgen05.commit)       MMAs of tile i done: A free, TMEM ready
-//   mb_tfree (epilogue thread 0)    TMEM of tile i read: MMAs of i + 1 may start
-//   mb_scale (converter thread 0)   the scale of tile i is in tile_scale[i & 1]
+// Handoffs (each mbarrier phase completes once per tile, or once per two
+// tiles for m_scale[b]; no waiter can fall two phases behind, because every
+// completion of a phase needs the waiter's previous phase to have been
+// consumed upstream):
+//   m_raw    bulk copies -> converters    the raw tile is in shared memory
+//   m_ready[s]  converter -> MMA          A slice s of tile i written
+//   m_free[s]   tcgen05.commit -> converter   the MMAs of tile i that read
+//            slice s are done (the last ones, of half 1)
+//   m_scale[i & 1]  converter -> epilogue  (doubles) scale of tile i in tile_scale[i & 1]
+//   m_full[h]  tcgen05.commit -> epilogue   MMAs of half h of tile i done
+//   m_tfree[h] epilogue (256 arrivals) -> MMA   half h of tile i read
 template <bool FIX>
-__global__ void __launch_bounds__(OZ_THREADS, 1)
+__global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registers
     k_fused5_oz(double2* __restrict__ psi, i64 ntiles, const __grid_constant__ OzGeom geo,
-                const __grid_constant__ OzGate G, int* __restrict__ err) {
+                const __grid_constant__ OzGate G, int* __restrict__ err, const uint32_t* __restrict__ fix_in,
+                uint32_t* __restrict__ fix_out, uint32_t* __restrict__ fix_zero) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t mb_full, mb_tfree, mb_scale;
+  __shared__ __align__(8) uint64_t m_raw, m_ready[OZ_NSLICE], m_free[OZ_NSLICE], m_scale[2], m_full[2], m_tfree[2],
+      m_drain;
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag;      // set by either group on a failed wait
-  __shared__ int c_stop, e_stop;  // each group's decision, written by its thread 0 before its barrier
-  __shared__ uint32_t red[OZ_GROUP / 32], red_hi[OZ_GROUP / 32];
+  __shared__ int abort_flag;  // set by any role on a failed wait
+  __shared__ int c_stop[2];   // the converters' decisions, written by their thread 0 before their barriers
+  __shared__ uint32_t red[OZ_CONV_WARPS];
   __shared__ int tile_scale[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t s_base = smem_u32(sm);
-  const uint32_t mfull = smem_u32(&mb_full), mtfree = smem_u32(&mb_tfree), mscale = smem_u32(&mb_scale);
+  volatile int* abort_v = &abort_flag;
 
-  // B slices: stacked row 64 j + n holds digit j of realified row n
-  // (n = 2 r + re/im of output r), column k = 2 c + re/im of input c
+  // B slices: row 192 h + 32 j + n' holds digit j of realified output row
+  // n = 32 h + n' (n = 2 r + re/im of output r), column k = 2 c + re/im of
+  // input c
   for (int e = tid; e < 64 * 64; e += OZ_THREADS) {
     const int n = e >> 6, k = e & 63, r = n >> 1, c = k >> 1;
     double v;
@@ -379,14 +536,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     else v = (k & 1) == 0 ? G.ui[r][c] : G.ur[r][c];
     int d[OZ_NSLICE];
     oz_digits(v, G.fexp[r], d);
+    const int hb = 192 * (n >> 5) + (n & 31);
 #pragma unroll
-    for (int j = 0; j < OZ_NSLICE; ++j) *(uint16_t*)(sm + OZ_OFF_B + oz_boff(64 * j + n, k)) = (uint16_t)oz_bf16(d[j]);
+    for (int j = 0; j < OZ_NSLICE; ++j)
+      *(uint16_t*)(sm + OZ_OFF_B + oz_boff(hb + 32 * j, k)) = (uint16_t)oz_bf16(d[j]);
   }
   if (tid == 0) {
     abort_flag = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mfull));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mtfree));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mscale));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_raw)));
+    for (int k = 0; k < OZ_NSLICE; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_ready[k])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_free[k])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_drain)));
+    for (int h = 0; h < 2; ++h) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_scale[h])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_full[h])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&m_tfree[h])), "r"(OZ_EPI));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
@@ -394,194 +561,206 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                  "r"(OZ_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // B slices -> tensor-core reads
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_base;
   const uint32_t a_lbo = geo.a_lbo;
   const int my_rest = lane < geo.nrest ? geo.rest[lane] : -1;
-  const int g = tid & (OZ_GROUP - 1);  // thread within its group
-  const i64 toff = (i64)(g & 127) + ((g >> 7) ? geo.g7 : 0);
+  // fixed point: the launch's shift from the OR of the state's |high words|
+  // (largest |X| < 2^(33 + ph) <= 2^(47 + sh)); this launch ORs its outputs
+  // into fix_out and clears fix_zero, the word the next launch ORs into
+  int fix_sh = 0;
+  if (FIX) {
+    const uint32_t m = *fix_in;
+    const int ph = m ? 31 - __clz((int)m) : -1;
+    fix_sh = ph > 14 ? ph - 14 : 0;
+    if (blockIdx.x == 0 && tid == 0) *fix_zero = 0;
+  }
 
-  if (warp < OZ_GROUP / 32) {
+  if (warp < OZ_CONV_WARPS) {
     // ---------------------------------------------------------- converters
+    // The raw tile arrives in shared memory by bulk copies issued one tile
+    // ahead (warp 0, one 2 KB run per lane), so the loads of the next tile
+    // are in flight while this one converts, with no registers held.  A
+    // thread reads its 16 amplitudes, turns them into their digit words Z
+    // (oz_zdigits) in registers and frees the raw tile for the next copy;
+    // then it writes digit slice s as soon as the previous tile's MMAs that
+    // read slice s are done, so the slices follow the MMAs one by one.
+    const int g = tid;  // 0..255
     const uint32_t aoff = geo.aoff_lo[g];
-    double2 v[OZ_STEPS];
+    const uint32_t mraw = smem_u32(&m_raw);
+    const uint32_t raw = s_base + OZ_OFF_RAW;
+    // run lane of warp 0: 2 r + hi, r = lane >> 1
+    const i64 run_off = ((lane & 1) ? geo.g7 : 0) + geo.ghi[lane >> 1];
+    auto issue_copy = [&](i64 tt) {  // warp 0, all lanes
+      const i64 tb = tile_base(tt, lane, my_rest);
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mraw), "r"((uint32_t)OZ_RAW_BYTES)
+                     : "memory");
+      __syncwarp();
+      oz_copy_run(raw + lane * OZ_RUN, psi + tb + run_off, mraw);
+    };
     i64 t = blockIdx.x;
-    if (t < ntiles) {
-      const double2* src = psi + tile_base(t, lane, my_rest) + toff;
-#pragma unroll
-      for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
+    int copies = 0, consumed = 0;  // raw-tile copies issued (by warp 0) and tiles whose copy was waited for
+    if (warp == 0 && t < ntiles) {
+      issue_copy(t);
+      copies = 1;
     }
-    int it = 0;
-    bool pending = false;  // thread 0: MMAs issued whose completion it has not seen
-    for (; t < ntiles; t += gridDim.x, ++it) {
-      // tile scale: doubles -- the largest biased exponent among the tile's
-      // 8192 values; fixed point -- the top bit of the OR of their magnitudes
-      uint32_t m = 0, mh = 0;
-      if (FIX) {
-        uint64_t o = 0;
+    for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
+      // this tile's raw values -> registers
+      const bool got = oz_wait(mraw, (uint32_t)it & 1, abort_v);
+      uint64_t zr[OZ_STEPS], zi[OZ_STEPS];
+#pragma unroll
+      for (int r = 0; r < OZ_STEPS; ++r) {
+        const double2 v = *(const double2*)(sm + OZ_OFF_RAW + (2 * r + (g >> 7)) * OZ_RUN + (g & 127) * 16);
+        zr[r] = oz_dbits(v.x);
+        zi[r] = oz_dbits(v.y);
+      }
+      if (!got) *abort_v = 1;
+      int scale = 0;  // exm (doubles): the largest biased exponent of the tile
+      if (!FIX) {
+        uint32_t m = 0;
 #pragma unroll
         for (int r = 0; r < OZ_STEPS; ++r) {
-          const int64_t a = (int64_t)oz_dbits(v[r].x), b = (int64_t)oz_dbits(v[r].y);
-          o |= (uint64_t)(a < 0 ? -a : a) | (uint64_t)(b < 0 ? -b : b);
-        }
-        m = __reduce_or_sync(0xffffffffu, (uint32_t)o);
-        mh = __reduce_or_sync(0xffffffffu, (uint32_t)(o >> 32));
-      } else {
-#pragma unroll
-        for (int r = 0; r < OZ_STEPS; ++r) {
-          m = max(m, (uint32_t)(oz_dbits(v[r].x) >> 32) & 0x7FF00000u);
-          m = max(m, (uint32_t)(oz_dbits(v[r].y) >> 32) & 0x7FF00000u);
+          m = max(m, (uint32_t)(zr[r] >> 32) & 0x7FF00000u);
+          m = max(m, (uint32_t)(zi[r] >> 32) & 0x7FF00000u);
         }
         m = __reduce_max_sync(0xffffffffu, m);
+        if (lane == 0) red[warp] = m;
       }
-      if (lane == 0) {
-        red[warp] = m;
-        red_hi[warp] = mh;
-      }
-      // the A slices are free once the MMAs of the previous tile are done
-      if (g == 0) {
-        bool bad = abort_flag != 0;
-        if (!bad && pending) {
-          if (mbar_wait(mfull, (uint32_t)(it - 1) & 1)) pending = false;
-          else bad = true;
-        }
-        if (bad) abort_flag = 1;
-        c_stop = bad;
-      }
+      if (g == 0) c_stop[0] = *abort_v;
+      // generic reads of the raw tile before the copy engine rewrites it
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       oz_bar(1);
-      if (c_stop) break;
-      int scale;  // exm (doubles) or sh (fixed point)
+      if (c_stop[0]) break;
+      if (warp == 0 && t + gridDim.x < ntiles) {
+        issue_copy(t + gridDim.x);
+        copies = it + 2;
+      }
       if (FIX) {
-        uint64_t ot = 0;
+        const int64_t bias = oz_fix_bias(fix_sh);
 #pragma unroll
-        for (int w = 0; w < OZ_GROUP / 32; ++w) ot |= ((uint64_t)red_hi[w] << 32) | red[w];
-        const int p = ot ? 63 - oz_clz64(ot) : -1;
-        scale = p > 46 ? p - 46 : 0;
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          zr[r] = oz_fix_z((int64_t)zr[r], fix_sh, bias);
+          zi[r] = oz_fix_z((int64_t)zi[r], fix_sh, bias);
+        }
       } else {
         uint32_t mx = red[0];
 #pragma unroll
-        for (int w = 1; w < OZ_GROUP / 32; ++w) mx = max(mx, red[w]);
+        for (int w = 1; w < OZ_CONV_WARPS; ++w) mx = max(mx, red[w]);
         scale = (int)(mx >> 20);
-      }
-      // digits -> A slices (one (re, im) bf16 pair per slice and amplitude)
 #pragma unroll
-      for (int r = 0; r < OZ_STEPS; ++r) {
-        float dre[OZ_NSLICE], dim[OZ_NSLICE];
-        if (FIX) {
-          oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].x), scale), dre);
-          oz_digits_f(oz_fix47_fix((int64_t)oz_dbits(v[r].y), scale), dim);
-        } else {
-          oz_digits_f(oz_fix47(v[r].x, scale), dre);
-          oz_digits_f(oz_fix47(v[r].y, scale), dim);
-        }
-        unsigned char* a = sm + OZ_OFF_A + aoff + geo.aoff_hi[r];
-#pragma unroll
-        for (int s = 0; s < OZ_NSLICE; ++s) *(uint32_t*)(a + s * OZ_A_SLICE) = oz_pack(dre[s], dim[s]);
-      }
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      oz_bar(1);
-      // prefetch the next tile into registers (the digits are in shared
-      // memory now); issued before the MMAs, whose issue blocks thread 0 and
-      // with it the rest of warp 0, so that the loads run under the MMAs
-      {
-        const i64 tn = t + gridDim.x;
-        if (tn < ntiles) {
-          const double2* src = psi + tile_base(tn, lane, my_rest) + toff;
-#pragma unroll
-          for (int r = 0; r < OZ_STEPS; ++r) v[r] = src[geo.ghi[r]];
+        for (int r = 0; r < OZ_STEPS; ++r) {
+          zr[r] = (uint64_t)oz_fix47(oz_bitsd(zr[r]), scale) + OZ_C5;
+          zi[r] = (uint64_t)oz_fix47(oz_bitsd(zi[r]), scale) + OZ_C5;
         }
       }
-      if (g == 0) {
-        // the MMAs overwrite TMEM: wait until the epilogue has read tile it - 1
-        bool ok = it == 0 || mbar_wait(mtfree, (uint32_t)(it - 1) & 1);
+      // slice by slice, each once the previous tile's MMAs on it are done
+      bool ok = true;
+#pragma unroll
+      for (int s = 0; s < OZ_NSLICE; ++s) {
+        ok = ok && (it == 0 || oz_wait(smem_u32(&m_free[s]), (uint32_t)(it - 1) & 1, abort_v));
         if (ok) {
-          tile_scale[it & 1] = scale;
-          oz_arrive(mscale);
-          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
-          for (int s = 0; s < 4; ++s) {  // K-steps of 16
-            const uint32_t bs = s_base + OZ_OFF_B + s * 2 * OZ_B_LBO;
-            const uint64_t b0 = smem_desc(bs, OZ_B_LBO, OZ_B_SBO);                    // B rows 0..
-            const uint64_t b256 = smem_desc(bs + 32 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 256..
-            const uint64_t b320 = smem_desc(bs + 40 * OZ_B_SBO, OZ_B_LBO, OZ_B_SBO);  // B rows 320..
-#pragma unroll
-            for (int i = 0; i < OZ_NSLICE; ++i) {
-              const uint64_t adesc = smem_desc(s_base + OZ_OFF_A + i * OZ_A_SLICE + s * 2 * a_lbo, a_lbo, OZ_A_SBO);
-              const int nrows = 64 * (i <= 1 ? OZ_NSLICE : OZ_NLEVEL - i);  // B slices 0..min(5, 6 - i)
-              const uint32_t acc = (i > 0 || s > 0) ? 1u : 0u;
-              if (s == 0 && i == 1) {
-                // levels 1..5 accumulate onto slice 0's products; level 6 starts here
-                oz_mma(tmem + 64, adesc, b0, oz_idesc(256), 1u);
-                oz_mma(tmem + 64 + 256, adesc, b256, oz_idesc(64), 1u);
-                oz_mma(tmem + 64 + 320, adesc, b320, oz_idesc(64), 0u);
-              } else {
-                oz_mma(tmem + 64 * i, adesc, b0, oz_idesc(nrows < 256 ? nrows : 256), acc);
-                if (nrows > 256) oz_mma(tmem + 64 * i + 256, adesc, b256, oz_idesc(nrows - 256), acc);
-              }
-            }
-          }
-          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mfull)
-                       : "memory");
-          pending = true;
+          for (int r = 0; r < OZ_STEPS; ++r)
+            *(uint32_t*)(sm + OZ_OFF_A + oz_slot(s) + aoff + geo.aoff_hi[r]) =
+                oz_pack(oz_zdigit(zr[r], s), oz_zdigit(zi[r], s));
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         } else {
-          abort_flag = 1;
+          *abort_v = 1;
         }
+        oz_bar(1);
+        if (g == 0 && !*abort_v) oz_arrive(smem_u32(&m_ready[s]));
       }
+      if (!FIX && g == 0 && ok) {
+        tile_scale[it & 1] = scale;  // read by the epilogue of tile it - 2 long ago
+        oz_arrive(smem_u32(&m_scale[it & 1]));
+      }
+      if (g == 0) c_stop[1] = *abort_v;
+      oz_bar(1);
+      if (c_stop[1]) break;
+      consumed = it + 1;
     }
-    // on an abort, give the last issued MMAs one more bounded wait so that
-    // tensor memory is not freed under them
-    if (g == 0 && pending) mbar_wait(mfull, (uint32_t)(it - 1) & 1);
-  } else {
+    // on an abort, a copy may still be writing the raw tile: wait for it
+    // (bounded) before the CTA's shared memory is released
+    if (g == 0 && copies > consumed) mbar_wait(mraw, (uint32_t)(copies - 1) & 1);
+  } else if (warp < OZ_MMA_WARP) {
     // ------------------------------------------------------------ epilogue
-    const int ew = warp - OZ_GROUP / 32;  // TMEM sub-partition ew & 3, column half ew >> 2
-    const int erow = 32 * (ew & 3) + lane;
-    const int ehalf = ew >> 2;
-    const uint32_t trow = tmem + ((uint32_t)(32 * (ew & 3)) << 16);
+    const int q = warp & 3;                     // TMEM lane quarter (warp mod 4)
+    const int cg = (warp - OZ_CONV_WARPS) >> 2;  // reals 16 cg .. 16 cg + 15 of each half
+    const int erow = 32 * q + lane;
+    const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16);
     const i64 myrow = geo.rowoff[erow];
+    const OzShift fsh = oz_shift(fix_sh + G.fexp[0] - 1029);  // fixed point: one shift per launch
+    uint32_t orm = 0;  // fixed point: OR of the outputs' |high word| (the next launch's shift)
     int it = 0;
+    bool failed = false;
     for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-      if (g == 0) {
-        const uint32_t par = (uint32_t)it & 1;
-        const bool bad = abort_flag || !mbar_wait(mscale, par) || !mbar_wait(mfull, par);
-        if (bad) abort_flag = 1;
-        e_stop = bad;
-      }
-      oz_bar(2);
-      if (e_stop) break;
-      const int scale = tile_scale[it & 1];
-      double2* dst = psi + tile_base(t, lane, my_rest) + myrow;
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      // combine the seven levels of 8 reals (4 amplitudes) at a time
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        float acc[OZ_NLEVEL][8];
-#pragma unroll
-        for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(trow + 64 * l + 32 * ehalf + 8 * q, acc[l]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          const int c = 16 * ehalf + 4 * q + (e >> 1);  // output amplitude (permuted block index)
-          float are[OZ_NLEVEL], aim[OZ_NLEVEL];
-#pragma unroll
-          for (int l = 0; l < OZ_NLEVEL; ++l) {
-            are[l] = acc[l][e];
-            aim[l] = acc[l][e + 1];
-          }
-          if (FIX) {
-            const OzShift k = oz_shift(scale + G.fexp[c] - 1029);
-            dst[geo.coloff[c]] = make_double2(oz_bitsd((uint64_t)oz_combine_fix(are, k)),
-                                              oz_bitsd((uint64_t)oz_combine_fix(aim, k)));
-          } else {
-            const int sc = scale + G.fexp[c] - 2098;
-            dst[geo.coloff[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
-          }
+      int scale = 0;
+      if (!FIX) {
+        if (!__all_sync(0xffffffffu, oz_wait(smem_u32(&m_scale[it & 1]), (uint32_t)(it >> 1) & 1, abort_v))) {
+          failed = true;
+          break;
         }
+        scale = tile_scale[it & 1];
       }
+      double2* dst = psi + tile_base(t, lane, my_rest) + myrow;
+      if (!__all_sync(0xffffffffu, oz_wait(smem_u32(&m_full[0]), (uint32_t)it & 1, abort_v))) {
+        failed = true;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (cg == 0) oz_epi_half<FIX, 0, 0>(dst, trow, geo, G, fsh, scale, orm);
+      else oz_epi_half<FIX, 0, 1>(dst, trow, geo, G, fsh, scale, orm);
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      oz_bar(2);
-      if (g == 0) oz_arrive(mtfree);  // TMEM of this tile read: the next MMAs may start
+      oz_arrive(smem_u32(&m_tfree[0]));  // half 0 read: the next tile's MMAs may write it
+      if (!__all_sync(0xffffffffu, oz_wait(smem_u32(&m_full[1]), (uint32_t)it & 1, abort_v))) {
+        failed = true;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (cg == 0) oz_epi_half<FIX, 1, 0>(dst, trow, geo, G, fsh, scale, orm);
+      else oz_epi_half<FIX, 1, 1>(dst, trow, geo, G, fsh, scale, orm);
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      oz_arrive(smem_u32(&m_tfree[1]));
+    }
+    if (failed) *abort_v = 1;
+    if (FIX) {
+      orm = __reduce_or_sync(0xffffffffu, orm);
+      if (lane == 0 && orm) atomicOr(fix_out, orm);
+    }
+  } else if (lane == 0) {
+    // ---------------------------------------------------------------- MMAs
+    bool issued = false, ok = true;
+    int it = 0;
+    for (i64 t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+      const uint32_t par = (uint32_t)it & 1, prev = (uint32_t)(it - 1) & 1;
+      ok = it == 0 || oz_wait(smem_u32(&m_tfree[0]), prev, abort_v);
+      for (int s = 0; s < OZ_NSLICE && ok; ++s) {
+        ok = oz_wait(smem_u32(&m_ready[s]), par, abort_v);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        oz_issue(s_base, tmem, a_lbo, 0, s, s + 1);
+        issued = true;
+      }
+      if (!ok) break;
+      oz_commit(smem_u32(&m_full[0]));
+      ok = it == 0 || oz_wait(smem_u32(&m_tfree[1]), prev, abort_v);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      for (int s = 0; s < OZ_NSLICE; ++s) {
+        oz_issue(s_base, tmem, a_lbo, 1, s, s + 1);
+        oz_commit(smem_u32(&m_free[s]));  // slice s may be rewritten once these are done
+      }
+      oz_commit(smem_u32(&m_full[1]));
+    }
+    if (!ok) *abort_v = 1;
+    // every issued MMA completes before tensor memory is freed (bounded)
+    if (issued) {
+      oz_commit(smem_u32(&m_drain));
+      mbar_wait(smem_u32(&m_drain), 0);
     }
   }
   __syncthreads();
@@ -671,8 +850,10 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
 }
 
 // permuted block U'[r'][c'] = U[idx[r']][idx[c']] (see make_oz_geom) and the
-// digit scale of each output row
-void make_oz_gate(const GateOp& g, const int cbit[5], OzGate* G) {
+// digit scale of each output row; uniform: every row takes the scale of the
+// largest entry of the block (the fixed-point kernel's epilogue then shifts
+// every output of a tile alike)
+void make_oz_gate(const GateOp& g, const int cbit[5], OzGate* G, bool uniform) {
   int idx[32];
   for (int c = 0; c < 32; ++c) {
     idx[c] = 0;
@@ -689,6 +870,10 @@ void make_oz_gate(const GateOp& g, const int cbit[5], OzGate* G) {
     }
     G->fexp[r] = (int)((oz_dbits(mx) >> 52) & 0x7FF);
   }
+  if (uniform) {
+    const int fm = *std::max_element(G->fexp, G->fexp + 32);
+    for (int r = 0; r < 32; ++r) G->fexp[r] = fm;
+  }
 }
 
 }  // namespace
@@ -696,8 +881,16 @@ void make_oz_gate(const GateOp& g, const int cbit[5], OzGate* G) {
 int* qgb_tc_err_flag();  // qgb_tc.cu
 
 // Uncontrolled 5-qubit dense block on a complex128 state of n >= 12 qubits;
-// fix: the state is in the fixed-point format (oz_to_fix).
-int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix) {
+// fix: the state is in the fixed-point format (oz_to_fix), and fix_words
+// holds the three words of the launch shifts of a chain: the launch reads
+// word b % 3 (the OR of the state's |high words|), ORs its outputs into
+// word (b + 1) % 3 and clears word (b + 2) % 3 for the launch after.
+int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix, uint32_t* fix_words,
+                         int b) {
+  if (fix && !fix_words) {
+    qgb_set_error("qgb_launch_fused5_oz: the fixed-point format needs the chain's shift words");
+    return QGB_ERR_INVALID;
+  }
   if (g.tbits.size() != 5 || !g.cbits.empty() || n < 12) {
     qgb_set_error("qgb_apply_fused5_tc: complex128 needs an uncontrolled 5-qubit dense block on >= 12 qubits");
     return QGB_ERR_INVALID;
@@ -708,7 +901,7 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
   OzGate* G = new OzGate();
   int cbit[5];
   make_oz_geom(n, g.tbits, geo, cbit);
-  make_oz_gate(g, cbit, G);
+  make_oz_gate(g, cbit, G, fix);
   static bool attr[2] = {false, false};
   if (!attr[fix]) {
     cudaFuncSetAttribute(fix ? k_fused5_oz<true> : k_fused5_oz<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -717,8 +910,12 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
   }
   const i64 ntiles = (i64)1 << (n - 12);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms());
-  if (fix) k_fused5_oz<true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err);
-  else k_fused5_oz<false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err);
+  if (fix)
+    k_fused5_oz<true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, fix_words + b % 3,
+                                                          fix_words + (b + 1) % 3, fix_words + (b + 2) % 3);
+  else
+    k_fused5_oz<false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, nullptr, nullptr,
+                                                           nullptr);
   delete G;
   delete geo;
   QGB_LAUNCH_CHECK("k_fused5_oz");
@@ -734,14 +931,27 @@ __host__ __device__ __forceinline__ int oz_scale_exp(double norm2) {
   return norm2 > 0 ? ((x + 1) >> 1) + 1 : 0;
 }
 
-__global__ void k_oz_scale(const double* __restrict__ norm2, int* __restrict__ e) { *e = oz_scale_exp(*norm2); }
+// the scale e, and the chain's first two shift words cleared
+__global__ void k_oz_scale(const double* __restrict__ norm2, int* __restrict__ e, uint32_t* __restrict__ fixw) {
+  *e = oz_scale_exp(*norm2);
+  fixw[0] = 0;
+  fixw[1] = 0;
+}
 
-__global__ void k_oz_to_fix(double2* __restrict__ psi, i64 N, const int* __restrict__ e_ptr) {
+// doubles -> fixed point; fixw[0] collects the OR of the values' |high
+// words| (the first block's shift)
+__global__ void k_oz_to_fix(double2* __restrict__ psi, i64 N, const int* __restrict__ e_ptr,
+                            uint32_t* __restrict__ fixw) {
   const int e = *e_ptr;
+  uint32_t m = 0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x) {
     const double2 v = psi[i];
-    psi[i] = make_double2(oz_bitsd((uint64_t)oz_to_fix(v.x, e)), oz_bitsd((uint64_t)oz_to_fix(v.y, e)));
+    const int64_t xr = oz_to_fix(v.x, e), xi = oz_to_fix(v.y, e);
+    m |= (uint32_t)abs((int32_t)((uint64_t)xr >> 32)) | (uint32_t)abs((int32_t)((uint64_t)xi >> 32));
+    psi[i] = make_double2(oz_bitsd((uint64_t)xr), oz_bitsd((uint64_t)xi));
   }
+  m = __reduce_or_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicOr(fixw, m);
 }
 
 __global__ void k_oz_from_fix(double2* __restrict__ psi, i64 N, const int* __restrict__ e_ptr) {
@@ -776,6 +986,7 @@ struct OzChainScratch {
   double* norm = nullptr;
   int* e = nullptr;
   void* red = nullptr;
+  uint32_t* fixw = nullptr;  // the three shift words of the fixed-point launches
 };
 OzChainScratch g_oz_default;
 std::mutex g_oz_mu;
@@ -785,6 +996,7 @@ int oz_scratch_alloc(OzChainScratch* c) {
   QGB_TRY_CUDA(cudaMalloc(&c->norm, sizeof(double)));
   QGB_TRY_CUDA(cudaMalloc(&c->e, sizeof(int)));
   QGB_TRY_CUDA(cudaMalloc(&c->red, qgb_norm_scratch_bytes()));
+  QGB_TRY_CUDA(cudaMalloc(&c->fixw, 3 * sizeof(uint32_t)));
   return QGB_OK;
 }
 }  // namespace
@@ -837,6 +1049,7 @@ int qgb_oz_stream_release(cudaStream_t s) {
   cudaFree(it->second.norm);
   cudaFree(it->second.e);
   cudaFree(it->second.red);
+  cudaFree(it->second.fixw);
   g_oz_streams.erase(it);
   return QGB_OK;
 }
@@ -851,14 +1064,14 @@ int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& block
   if (st) return st;
   st = qgb_norm2(state, n, QGB_C128, cs->norm, cs->red, (void*)s);
   if (st) return st;
-  k_oz_scale<<<1, 1, 0, s>>>(cs->norm, cs->e);
+  k_oz_scale<<<1, 1, 0, s>>>(cs->norm, cs->e, cs->fixw);
   QGB_LAUNCH_CHECK("k_oz_scale");
   const i64 N = (i64)1 << n;
   const int grid = (int)std::min<i64>((N + 255) / 256, (i64)qgb_num_sms() * 8);
-  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, cs->e);
+  k_oz_to_fix<<<grid, 256, 0, s>>>((double2*)state, N, cs->e, cs->fixw);
   QGB_LAUNCH_CHECK("k_oz_to_fix");
-  for (const GateOp* g : blocks) {
-    st = qgb_launch_fused5_oz(state, n, *g, s, true);
+  for (size_t b = 0; b < blocks.size(); ++b) {
+    st = qgb_launch_fused5_oz(state, n, *blocks[b], s, true, cs->fixw, (int)(b % 3));
     if (st) return st;
   }
   k_oz_from_fix<<<grid, 256, 0, s>>>((double2*)state, N, cs->e);

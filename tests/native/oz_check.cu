@@ -47,14 +47,15 @@ static int wavefronts(const uint32_t* off, int width) {
 }
 
 // One launch of k_fused5_oz<true> replayed on a fixed-point state (X holds
-// the re, im integers of each amplitude): tile shift from the OR of the
-// magnitudes, oz_digits_f, exact level sums, oz_combine_fix, direct stores.
+// the re, im integers of each amplitude): one shift for the launch from the
+// OR of the state's high words' magnitudes, byte digits (oz_fix_z,
+// oz_zdigits), exact level sums, oz_combine_fix, direct stores.
 static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, int* exact_fails) {
   OzGeom* geo = new OzGeom();
   OzGate* G = new OzGate();
   int cbit[5];
   make_oz_geom(n, g.tbits, geo, cbit);
-  make_oz_gate(g, cbit, G);
+  make_oz_gate(g, cbit, G, true);
   static int Bd[OZ_NSLICE][64][64];
   for (int nn = 0; nn < 64; ++nn)
     for (int k = 0; k < 64; ++k) {
@@ -69,29 +70,38 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
   for (int row = 0; row < 128; ++row)
     for (int c = 0; c < 32; ++c)
       dec[(c >> 2) * geo->a_lbo + (row >> 3) * OZ_A_SBO + (row & 7) * 16 + (c & 3) * 4] = {row, c};
+  // the launch's shift: top bit of the OR of |high word| over the state
+  // (written by the previous launch or the conversion), as the kernel reads it
+  uint32_t o = 0;
+  uint64_t exact = 0;
+  for (size_t i = 0; i < X.size(); ++i) {
+    o |= (uint32_t)std::abs((int32_t)((uint64_t)X[i] >> 32));
+    exact |= (uint64_t)(X[i] < 0 ? -X[i] : X[i]);
+  }
+  const int ph = o ? 31 - __builtin_clz(o) : -1;
+  const int sh = ph > 14 ? ph - 14 : 0;
+  // the shift keeps every value within 47 bits, and is at most one above
+  // the exact one
+  {
+    const int p = exact ? 63 - oz_clz64(exact) : -1;
+    if ((exact >> sh) >= (1ull << 47) || sh > (p > 46 ? p - 46 : 0) + 1) (*exact_fails)++;
+  }
+  const int64_t bias = oz_fix_bias(sh);
   const i64 ntiles = (i64)1 << (n - 12);
+  std::vector<int64_t> Xout(X.size());
   for (i64 t = 0; t < ntiles; ++t) {
     const i64 base = host_tile_base(t, *geo);
     auto gidx = [&](int tid, int r) {
       return base + (tid & 127) + ((tid >> 7) ? geo->g7 : 0) + geo->ghi[r];
     };
-    uint64_t o = 0;
-    for (int r = 0; r < OZ_STEPS; ++r)
-      for (int tid = 0; tid < OZ_GROUP; ++tid)
-        for (int part = 0; part < 2; ++part) {
-          const int64_t a = X[2 * gidx(tid, r) + part];
-          o |= (uint64_t)(a < 0 ? -a : a);
-        }
-    const int p = o ? 63 - oz_clz64(o) : -1;
-    const int sh = p > 46 ? p - 46 : 0;
     static int Ad[OZ_NSLICE][128][64];
     for (int r = 0; r < OZ_STEPS; ++r)
       for (int tid = 0; tid < OZ_GROUP; ++tid) {
         const auto rc = dec[geo->aoff_lo[tid] + geo->aoff_hi[r]];
         const i64 gi = gidx(tid, r);
         float fre[OZ_NSLICE], fim[OZ_NSLICE];
-        oz_digits_f(oz_fix47_fix(X[2 * gi], sh), fre);
-        oz_digits_f(oz_fix47_fix(X[2 * gi + 1], sh), fim);
+        oz_zdigits(oz_fix_z(X[2 * gi], sh, bias), fre);
+        oz_zdigits(oz_fix_z(X[2 * gi + 1], sh, bias), fim);
         int dre[OZ_NSLICE], dim[OZ_NSLICE];
         for (int s = 0; s < OZ_NSLICE; ++s) {
           dre[s] = (int)fre[s];
@@ -116,10 +126,11 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
             acc[l] = (float)sum;
           }
           // the epilogue's direct store of (row, c)
-          X[2 * (base + geo->rowoff[row] + geo->coloff[c]) + part] =
-              oz_combine_fix(acc, oz_shift(sh + G->fexp[c] - 1029));
+          Xout[2 * (base + geo->rowoff[row] + geo->coloff[c]) + part] =
+              oz_combine_fix(acc, oz_shift(sh + G->fexp[0] - 1029));
         }
   }
+  X = Xout;
   delete geo;
   delete G;
 }
@@ -226,7 +237,7 @@ int main() {
       OzGate* G = new OzGate();
       int cbit[5];
       make_oz_geom(n, tb, geo, cbit);
-      make_oz_gate(g, cbit, G);
+      make_oz_gate(g, cbit, G, false);
       int t5 = 0;
       for (int b : tb) t5 += b < 5;
       const i64 N = (i64)1 << n;
@@ -265,7 +276,7 @@ int main() {
           oz_digits(v, G->fexp[r], d);
           for (int j = 0; j < OZ_NSLICE; ++j) {
             Bd[j][nn][k] = d[j];
-            if (oz_boff(64 * j + nn, k) + 2 > 8 * OZ_B_LBO) exact_fails++;
+            if (oz_boff(192 * (nn >> 5) + 32 * j + (nn & 31), k) + 2 > 8 * OZ_B_LBO) exact_fails++;
           }
         }
       std::map<uint32_t, std::pair<int, int>> dec;  // A slice byte offset of (row, c) pair
