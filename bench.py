@@ -594,20 +594,27 @@ def run_qft20(args):
 def run_vqe24(args):
     """24-qubit hardware-efficient ansatz (10 layers RY+RZ + CNOT ladder, 480
     parameters), periodic TFIM h=1: energy and all 480 adjoint gradients."""
-    from oracle import numpy_ref as ref  # circuit factory and TFIM term list only
     from qibo_gb300 import Circuit, gates
     from qibo_gb300.adjoint import adjoint_gradient
     from qibo_gb300.backend import GB300Backend
 
     n, layers = 24, 10
     p = np.random.default_rng(24).uniform(-np.pi, np.pi, 2 * n * layers)
-    ham = ref.tfim_terms(n)
+    # periodic TFIM, h = 1 (hamiltonians/models.py:649-662): -sum Z_i Z_i+1 - sum X_i
+    ham = (["ZZ"] * n + ["X"] * n, [(i, (i + 1) % n) for i in range(n)] + [(i,) for i in range(n)],
+           [-1.0] * (2 * n))
     out = {}
     for dtype in ("complex128", "complex64"):
         b = GB300Backend(dtype)
         c = Circuit(n)
-        for nm, q, pp in ref.vqe_ops(n, layers, p):
-            c.add(getattr(gates, nm)(*q, *pp))
+        k = 0
+        for _ in range(layers):  # RY then RZ on every qubit, then a CNOT ladder
+            for q in range(n):
+                c.add(gates.RY(q, float(p[k])))
+                c.add(gates.RZ(q, float(p[k + 1])))
+                k += 2
+            for q in range(n - 1):
+                c.add(gates.CNOT(q, q + 1))
         times = []
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()

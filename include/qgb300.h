@@ -148,8 +148,10 @@ int qgb_plan_passes(int nqubits, int dtype, const qgb_op* ops, int nops, const d
  * significant).  QGB_ERR_UNSUPPORTED below the qubit minimum. */
 int qgb_apply_fused5_tc(void* state, int nqubits, int dtype, const int* qubits, const double* matrix, void* stream);
 /* *timed_out = 1 if a tensor-core launch since the previous call gave up
- * waiting for its MMAs (that launch stopped early and its output is
- * invalid); clears the flag.  Synchronising. */
+ * waiting for its MMAs or copies (that launch stopped early and its output
+ * is invalid); clears the flag.  Not synchronising: it reads a flag in
+ * mapped host memory, so call it after synchronising the streams whose
+ * launches it should cover. */
 int qgb_tc_status(int* timed_out);
 
 /* ---- measurement: Backend.calculate_probabilities (:2734-2758,
@@ -191,9 +193,11 @@ int qgb_sample_state(const void* state, int nqubits, int dtype, int64_t nshots, 
  * it, until exit), so m is limited to 20 (2^20 outcomes); larger m returns
  * QGB_ERR_INVALID.  Same outputs as qgb_sample for the same arguments.  The
  * first call on a device looks up that array's device address (do it before
- * any stream capture).  All calls share the one array: calls that can overlap
- * on the GPU (different streams without ordering) race and must not be
- * issued. */
+ * any stream capture); the address is kept per device, for the device's
+ * primary context (the one the CUDA runtime uses), the only context this
+ * entry point supports.  All calls share the one array: calls that can
+ * overlap on the GPU (different streams without ordering) race and must not
+ * be issued. */
 int qgb_sample_noalloc(const double* probs, int m, int64_t nshots, uint64_t seed, int64_t* samples,
                        int64_t* counts, void* stream);
 /* Raw Philox4x32-10 words: out[4t+e] = word e of philox(counter = (t_lo,

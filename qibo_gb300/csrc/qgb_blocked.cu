@@ -188,6 +188,7 @@ struct PassLaunch {
   size_t smem;
   i64 ntiles, blocks;
   int threads;
+  int status;  // QGB status of the shared-memory attribute
 };
 
 template <typename T>
@@ -195,14 +196,10 @@ PassLaunch<T> pass_launch(int n, int L, int m) {
   PassLaunch<T> pl;
   pl.ntiles = (i64)1 << (n - L);
   pl.smem = ((size_t)sizeof(typename T::S) << L) + (sizeof(i64) << (L - m));
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_pass<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_pass<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_pass_dev<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_pass_dev<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  pl.status = qgb_func_smem((const void*)k_pass<T, 2>, 200 * 1024);
+  if (!pl.status) pl.status = qgb_func_smem((const void*)k_pass<T, 5>, 200 * 1024);
+  if (!pl.status) pl.status = qgb_func_smem((const void*)k_pass_dev<T, 2>, 200 * 1024);
+  if (!pl.status) pl.status = qgb_func_smem((const void*)k_pass_dev<T, 5>, 200 * 1024);
   const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(4, (220 * 1024) / (pl.smem + 1024)));
   pl.blocks = std::min<i64>(pl.ntiles, (i64)qgb_num_sms() * per_sm);
   pl.threads = std::min(256, std::max(32, 1 << L));
@@ -222,6 +219,10 @@ int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vect
   PassParams<T>* P = new PassParams<T>();
   pack_params<T>(P, n, L, m, pass, ops);
   const PassLaunch<T> pl = pass_launch<T>(n, L, m);
+  if (pl.status) {
+    delete P;
+    return pl.status;
+  }
   if (pass_maxk(pass, ops) <= 2)
     k_pass<T, 2><<<(unsigned)pl.blocks, pl.threads, pl.smem, s>>>((typename T::G*)state, pl.ntiles, *P);
   else
@@ -363,6 +364,7 @@ void program_pack(Program* p) {
 template <typename T>
 int program_launches(Program* p, cudaStream_t s) {
   const PassLaunch<T> pl = pass_launch<T>(p->n, p->L, p->m);
+  if (pl.status) return pl.status;
   for (size_t i = 0; i < p->passes.size(); ++i) {
     const PassParams<T>* P = (const PassParams<T>*)((unsigned char*)p->dparams + i * p->pbytes);
     if (pass_maxk(p->passes[i], p->ops) <= 2)

@@ -43,6 +43,10 @@ void qgb_count_launch();
 
 int qgb_num_sms();
 
+// Raise the dynamic shared-memory limit of kernel func to bytes on the
+// current device, once per (kernel, device); thread-safe; a QGB status.
+int qgb_func_smem(const void* func, int bytes);
+
 // --------------------------------------------------------- complex math --
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));

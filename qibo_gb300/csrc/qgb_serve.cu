@@ -242,11 +242,8 @@ int batch_run(BatchCtx* c, const qgb_batch_item* items, int nitems, cudaStream_t
   QGB_TRY_CUDA(cudaMemcpyAsync(c->dev, c->host, off, cudaMemcpyHostToDevice, s));
   QGB_TRY_CUDA(cudaEventRecord(c->staged, s));
   const size_t smem = (sizeof(typename T::S) << maxn) + (sizeof(double) << maxn);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  const int sa = qgb_func_smem((const void*)k_batch<T>, 200 * 1024);
+  if (sa) return sa;
   const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (220 * 1024) / (smem + 4096)));
   const int blocks = std::max(1, std::min(nitems, qgb_num_sms() * per_sm));
   k_batch<T><<<blocks, 256, smem, s>>>((const DevItem*)c->dev, nitems, maxn);

@@ -6,6 +6,8 @@
 #include <cstdio>
 #include <atomic>
 #include <mutex>
+#include <set>
+#include <utility>
 
 #include "qgb_common.cuh"
 
@@ -39,6 +41,18 @@ int qgb_num_sms() {
     if (g_sms <= 0) g_sms = 152;
   }
   return g_sms;
+}
+
+int qgb_func_smem(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;  // (kernel, device)
+  int dev = 0;
+  QGB_TRY_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count({func, dev})) return QGB_OK;
+  QGB_TRY_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert({func, dev});
+  return QGB_OK;
 }
 
 int qgb_tc_prepare();  // qgb_tc128.cu: tensor-core device buffers

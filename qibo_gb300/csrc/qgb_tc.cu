@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
       // record the failure, give the in-flight MMAs one more bounded wait so
       // tensor memory is not freed under them, then leave
       if (tid == 0) {
-        atomicExch(err, 1);
+        *(volatile int*)err = 1;
         mbar_wait(mb, phase);
       }
       break;
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     __syncthreads();
     if (abort_flag) {
       if (tid == 0) {
-        atomicExch(err, 1);
+        *(volatile int*)err = 1;
         mbar_wait(mb, phase);
       }
       break;
@@ -474,17 +474,23 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 }
 
 namespace {
-int* g_tc_err = nullptr;
+int* g_tc_err = nullptr;       // device address of the flag
+int* g_tc_err_host = nullptr;  // the same word, page-locked host memory mapped into the device
 }  // namespace
 
-// Device flag the tensor-core kernels set when a bounded mbarrier wait gives
-// up; allocated and zeroed on first use, cleared by qgb_tc_status.
+// Flag the tensor-core kernels set when a bounded mbarrier wait gives up:
+// one word of mapped page-locked host memory, so the host reads it after a
+// stream synchronisation without a copy.  Allocated and zeroed on first use,
+// cleared by qgb_tc_status.
 int* qgb_tc_err_flag() {
   if (!g_tc_err) {
-    if (cudaMalloc(&g_tc_err, sizeof(int)) != cudaSuccess || cudaMemset(g_tc_err, 0, sizeof(int)) != cudaSuccess) {
+    if (cudaHostAlloc((void**)&g_tc_err_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&g_tc_err, g_tc_err_host, 0) != cudaSuccess) {
       qgb_set_error("tensor-core error flag: %s", cudaGetErrorString(cudaGetLastError()));
       g_tc_err = nullptr;
+      return nullptr;
     }
+    *(volatile int*)g_tc_err_host = 0;
   }
   return g_tc_err;
 }
@@ -666,14 +672,6 @@ int tcm_plan(const std::vector<int>& tbits) {
   return shfl > strided ? TCM_SHFL : TCM_STRIDED;
 }
 
-template <bool FULL>
-void set_tc_smem_attr() {
-  static bool done = false;
-  if (!done) {
-    cudaFuncSetAttribute(k_fused5_tc<FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    done = true;
-  }
-}
 }  // namespace
 
 int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
@@ -712,12 +710,16 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s) {
   if (gm) {
     k_fused5_tcm<<<blocks, TC_THREADS, TCM_SMEM, s>>>((float2*)state, ntiles, *gm, *G, err);
     delete gm;
-  } else if (geo->nbits == 12) {
-    set_tc_smem_attr<true>();
-    k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
   } else {
-    set_tc_smem_attr<false>();
-    k_fused5_tc<false><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
+    const bool full = geo->nbits == 12;
+    const int sa = qgb_func_smem(full ? (const void*)k_fused5_tc<true> : (const void*)k_fused5_tc<false>, TC_SMEM);
+    if (sa) {
+      delete G;
+      delete geo;
+      return sa;
+    }
+    if (full) k_fused5_tc<true><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
+    else k_fused5_tc<false><<<blocks, TC_THREADS, TC_SMEM, s>>>((float2*)state, ntiles, *geo, *G, err);
   }
   delete G;
   delete geo;
@@ -757,9 +759,10 @@ int qgb_tc_status(int* timed_out) {
     return QGB_ERR_INVALID;
   }
   *timed_out = 0;
-  if (g_tc_err) {
-    QGB_TRY_CUDA(cudaMemcpy(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
-    QGB_TRY_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
+  if (g_tc_err_host) {
+    volatile int* f = g_tc_err_host;
+    *timed_out = *f;
+    if (*timed_out) *f = 0;
   }
   return QGB_OK;
 }

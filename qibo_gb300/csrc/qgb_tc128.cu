@@ -764,7 +764,7 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
     }
   }
   __syncthreads();
-  if (tid == 0 && abort_flag) atomicExch(err, 1);  // a wait gave up: reported by qgb_tc_status
+  if (tid == 0 && abort_flag) *(volatile int*)err = 1;  // a wait gave up: reported by qgb_tc_status
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(OZ_TMEM_COLS));
 }
@@ -902,11 +902,11 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
   int cbit[5];
   make_oz_geom(n, g.tbits, geo, cbit);
   make_oz_gate(g, cbit, G, fix);
-  static bool attr[2] = {false, false};
-  if (!attr[fix]) {
-    cudaFuncSetAttribute(fix ? k_fused5_oz<true> : k_fused5_oz<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         OZ_SMEM);
-    attr[fix] = true;
+  const int sa = qgb_func_smem(fix ? (const void*)k_fused5_oz<true> : (const void*)k_fused5_oz<false>, OZ_SMEM);
+  if (sa) {
+    delete G;
+    delete geo;
+    return sa;
   }
   const i64 ntiles = (i64)1 << (n - 12);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms());
@@ -1012,7 +1012,8 @@ int qgb_tc_prepare() {
 }
 
 // Chain scratch of stream s, allocated on its first use outside a capture
-// (qgb_stream_create calls this so that the serving loop never allocates).
+// (qgb_stream_create calls this so that the serving loop never allocates);
+// a stream seen for the first time while it is being captured is refused.
 int qgb_oz_stream_scratch(cudaStream_t s, OzChainScratch** out) {
   int st = qgb_tc_prepare();
   if (st) return st;
@@ -1026,7 +1027,14 @@ int qgb_oz_stream_scratch(cudaStream_t s, OzChainScratch** out) {
   }
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   QGB_TRY_CUDA(cudaStreamIsCapturing(s, &cap));
-  if (cap != cudaStreamCaptureStatusNone) return QGB_OK;
+  if (cap != cudaStreamCaptureStatusNone) {
+    // sharing the default set would let two graphs replayed at once on
+    // different streams race on the chain's scale
+    qgb_set_error(
+        "complex128 block chains on a stream under capture need the stream's own scratch: create the stream with "
+        "qgb_stream_create, or run one complex128 circuit on it before capturing");
+    return QGB_ERR_INVALID;
+  }
   OzChainScratch c;
   st = oz_scratch_alloc(&c);
   if (st) return st;

@@ -75,7 +75,18 @@ class Runtime:
         return self._scratch
 
     def synchronize(self):
+        """Wait for the stream, then raise ``DeviceTimeout`` if a tensor-core
+        kernel gave up one of its bounded waits since the last check (its
+        output is invalid)."""
         check(self.lib.qgb_stream_sync(self.stream))
+        self.check_waits()
+
+    def check_waits(self):
+        flag = C.c_int(0)
+        check(self.lib.qgb_tc_status(C.byref(flag)))
+        if flag.value:
+            raise _lib.DeviceTimeout(_lib.QGB_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its MMAs or "
+                                     "copies (bounded wait); the state it wrote is invalid")
 
     def mem_info(self):
         f, t = C.c_size_t(), C.c_size_t()

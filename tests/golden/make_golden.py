@@ -2,7 +2,10 @@
 
 Run in a container that holds the reference source tree::
 
-    python tests/golden/make_golden.py [/path/to/qibo/src]
+    python tests/golden/make_golden.py /path/to/qibo/src
+
+(or with the source directory in the environment variable
+``QIBO_REFERENCE_SRC``).
 
 The reference needs two import shims outside its tree (both written to a
 temporary directory here): a ``qibo-<ver>.dist-info/METADATA`` so that
@@ -23,7 +26,7 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_SRC = "/root/reference/src"
+SRC_ENV = "QIBO_REFERENCE_SRC"
 
 
 def _import_reference(src: str):
@@ -76,7 +79,7 @@ def _gate(qibo, name, qubits, params):
     return cls(*qubits, *params)
 
 
-def main(src: str = DEFAULT_SRC):
+def main(src: str):
     qibo = _import_reference(src)
     from qibo import gates, Circuit
     from qibo.models import QFT
@@ -214,4 +217,7 @@ def main(src: str = DEFAULT_SRC):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_SRC)
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(SRC_ENV)
+    if not src:
+        sys.exit(f"usage: make_golden.py <qibo src directory> (or set {SRC_ENV})")
+    main(src)

@@ -137,16 +137,10 @@ def test_qibo_plugin_registration():
     to this package's MetaBackend (backends/__init__.py:325-350).  The
     backend object is built lazily: constructing it needs a GPU, so here
     only the provider lookup and class wiring are checked."""
-    import importlib.util
-    import sys
+    from conftest import import_reference
 
-    gold = os.path.join(ROOT, "tests", "golden", "make_golden.py")
-    spec = importlib.util.spec_from_file_location("make_golden", gold)
-    mg = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mg)
-    if not os.path.isdir(mg.DEFAULT_SRC) and "qibo" not in sys.modules:
+    if import_reference() is None:
         pytest.skip("reference qibo not importable here")
-    qibo = mg._import_reference(mg.DEFAULT_SRC)
     from qibo.backends import construct_backend
     from qibo.backends.numpy import NumpyBackend
 
@@ -185,3 +179,28 @@ def test_measurement_semantics_of_the_standalone_circuit():
     assert len(c.measurements) == 1
     with pytest.raises(NotImplementedError):
         gates.M(0, p0=0.1)
+
+
+def test_timeout_status_maps_to_device_timeout(monkeypatch):
+    """A QGB_ERR_TIMEOUT status becomes DeviceTimeout, and a tensor-core
+    kernel that gave up a bounded wait (the flag qgb_tc_status reports) is
+    raised at the next synchronisation, before its output is read.  The
+    failure is injected on the host (tests/host_device.py); no GPU runs."""
+    from host_device import HostLib
+
+    from qibo_gb300 import _lib
+    from qibo_gb300.device import DeviceState, Runtime
+
+    host = HostLib()
+    monkeypatch.setattr(_lib, "_lib", host)
+    monkeypatch.setattr(Runtime, "_instance", None)
+    host.error = b"bounded wait gave up"
+    with pytest.raises(_lib.DeviceTimeout, match="bounded wait gave up"):
+        _lib.check(_lib.QGB_ERR_TIMEOUT)
+    st = DeviceState.zero(3, "complex128")
+    np.testing.assert_array_equal(st.to_numpy(), np.eye(8)[0])
+    host.timed_out = 1
+    with pytest.raises(_lib.DeviceTimeout):
+        st.to_numpy()
+    # the flag is cleared once reported
+    np.testing.assert_array_equal(st.to_numpy(), np.eye(8)[0])
