@@ -305,6 +305,38 @@ def serving_sample(nreq: int, rates, baseline: bool = True):
     return out
 
 
+def analytic_check(backend, n, dtype, depth=DEPTH, seed=SEED):
+    """Max-abs error of the engine against a closed-form answer at the
+    benchmark's size: U3 on every qubit (a product state), the depth-20
+    brickwork and its inverse, with engine fusion; the product state must
+    come back.  Checked at 4096 random indices plus both ends."""
+    from qibo_gb300 import Circuit, gates
+
+    ang = np.random.default_rng(seed + 1).uniform(0, 2 * np.pi, (n, 3))
+    u = np.array([gates.U3(0, *a).matrix()[:, 0] for a in ang])
+    layer = [gates.U3(q, *ang[q]) for q in range(n)]
+    bw = brickwork_gates(n, depth, seed)
+    inv = []
+    for g in reversed(bw):
+        if type(g).__name__ == "U3":
+            th, ph, la = g.parameters
+            inv.append(gates.U3(g.target_qubits[0], -th, -la, -ph))
+        else:
+            inv.append(g)
+    c = Circuit(n)
+    c.add(layer + bw + inv)
+    st = backend.execute_circuit(c).state()
+    rng = np.random.default_rng(3)
+    idx = np.unique(np.concatenate([rng.integers(0, 2**n, 4096, dtype=np.int64), [0, 2**n - 1]]))
+    bits = (idx[:, None] >> (n - 1 - np.arange(n))[None, :]) & 1
+    want = np.prod(u[np.arange(n)[None, :], bits], axis=1)
+    err = float(np.max(np.abs(st.take(idx) - want)))
+    del st
+    return {"circuit": f"U3 on every qubit, the depth-{depth} brickwork (seed {seed}) and its inverse, engine fusion",
+            "answer": "the product state of the U3 layer (closed form)", "indices": int(idx.size),
+            "max_abs_error": err, "tolerance": 1e-12 if dtype == "complex128" else 1e-5}
+
+
 def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8):
     """complex64 legs of the brickwork circuit against complex128.
 
@@ -623,6 +655,8 @@ def run_brickwork(args):
             "e2e": {"value": plan_bytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": coef_bytes,
                     "d2h_bytes_per_step": NSHOTS * 8, "seconds": e2e_s}}
 
+    if rank == 0 and not args.quick:
+        line["analytic_check"] = analytic_check(backend, n, dtype)
     if dtype == "complex128" and rank == 0 and not args.quick:
         line["complex64"] = complex64_legs(args, n, circ, udescs, state, backend, ev, ndense, ncz)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

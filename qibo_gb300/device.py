@@ -146,6 +146,20 @@ class DeviceArray:
     def __getitem__(self, item):
         return self.to_numpy()[item]
 
+    def take(self, indices) -> np.ndarray:
+        """Elements at ``indices`` of the flat array, read with one small
+        copy each (a few amplitudes of a state too large to copy whole)."""
+        idx = np.asarray(indices, dtype=np.int64).ravel()
+        if idx.size and (idx.min() < 0 or idx.max() >= self.size):
+            raise IndexError(f"index out of range for {self.size} elements")
+        out = np.empty(idx.size, dtype=self.dtype)
+        item = self.dtype.itemsize
+        for k, i in enumerate(idx):
+            check(self.rt.lib.qgb_memcpy_d2h(out.ctypes.data + k * item, self.ptr + int(i) * item, item,
+                                             self.rt.stream))
+        self.rt.synchronize()
+        return out
+
     def __repr__(self):
         return f"DeviceArray(shape={self.shape}, dtype={self.dtype.name})"
 
