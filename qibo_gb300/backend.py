@@ -187,10 +187,23 @@ class GB300Methods:
         return result
 
     def execute_circuits(self, circuits, initial_states=None, nshots=1000, processes=None):
-        """Backend.execute_circuits (:2514): here sequential on the device."""
-        if initial_states is None:
-            initial_states = [None] * len(circuits)
-        return [self.execute_circuit(c, s, nshots) for c, s in zip(circuits, initial_states)]
+        """Backend.execute_circuits (:2514-2530, a host thread pool in the
+        reference) through the continuous-batching server
+        (``qibo_gb300.parallel.serve_circuits``): the circuits overlap on the
+        device, same-shape mid-sized circuits replay one captured graph.
+        ``processes`` is accepted and unused."""
+        from .parallel import serve_circuits
+
+        return serve_circuits(self, circuits, initial_states, nshots)
+
+    def server(self):
+        """The backend's ``serving.Server`` (created on first use)."""
+        srv = getattr(self, "_server", None)
+        if srv is None:
+            from .serving import Server
+
+            srv = self._server = Server(nslots=8)
+        return srv
 
     def execute_circuit_repeated(self, circuit, nshots, initial_state=None):
         """Backend.execute_circuit_repeated (backends/abstract.py:2532-2636)

@@ -76,9 +76,14 @@ class Circuit:
         c.add(other.queue)
         return c
 
-    def copy(self) -> "Circuit":
+    def copy(self, deep: bool = False) -> "Circuit":
+        """A circuit with the same gates (models/circuit.py ``copy``); with
+        ``deep`` the gates are copies, so changing their parameters leaves
+        this circuit's alone."""
+        import copy as _copy
+
         c = Circuit(self.nqubits)
-        c.add(list(self.queue))
+        c.add([_copy.deepcopy(g) for g in self.queue] if deep else list(self.queue))
         return c
 
     def invert(self) -> "Circuit":

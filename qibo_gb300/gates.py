@@ -110,12 +110,12 @@ class Gate:
     ncontrols = 0
 
     def __init__(self, *args, trainable: bool = True, **kwargs):
-        nq = len(args) - self.nparams
+        # parameters by keyword (theta, phi, lam: qibo's names) come after
+        # the positional ones
+        kw = tuple(kwargs.pop(key) for key in ("theta", "phi", "lam") if key in kwargs)
+        nq = len(args) - max(0, self.nparams - len(kw))
         qubits = tuple(int(q) for q in args[:nq])
-        params = tuple(args[nq:])
-        for key in ("theta", "phi", "lam"):
-            if key in kwargs:
-                params = params + (kwargs.pop(key),)
+        params = tuple(args[nq:]) + kw
         if kwargs.get("q") is not None:
             qubits = (int(kwargs.pop("q")),)
         self.name = type(self).__name__

@@ -11,9 +11,10 @@ scheduler
   launch through ``qgb_batch_run``, each CTA holding a whole state in shared
   memory and producing its output in the same kernel;
 * runs mid-sized circuits as shared-memory passes on their own stream
-  through a ``qgb_program`` per circuit shape and slot, whose launches are
-  captured once as a CUDA graph and replayed with new matrices for later
-  requests of the same shape;
+  through a ``qgb_program`` per circuit shape (a small pool of them, one per
+  request of that shape on the device at once), whose launches are captured
+  once as a CUDA graph and replayed with new matrices for later requests of
+  the same shape;
 * runs circuits of ``fuse_min_qubits`` qubits or more, whose device time
   dwarfs their launch overhead, through ``qgb_apply_circuit`` with engine
   fusion: blocks of five qubits on the tensor cores (complex64 3xTF32,
@@ -66,6 +67,7 @@ class Request:
     zmask: int = 0
     seed: int = 0
     arrival: float = 0.0
+    initial: object = None  # host state to start from instead of |0...0>
     result: object = None
     t_arrived: float = math.nan  # when the scheduler saw it arrive
     t_done: float = math.nan
@@ -245,6 +247,7 @@ class _Flight:
     buffers: list = field(default_factory=list)   # (ptr, nbytes)
     hostbufs: list = field(default_factory=list)  # (request, pinned array, view)
     kind: str = "large"
+    program: tuple = None  # (pool key, program) in use, returned on completion
 
 
 class Server:
@@ -270,11 +273,16 @@ class Server:
             self.events.append(e)
             self.batch_ctx.append(b)
         self.free_slots = list(range(self.nslots))
-        self.programs: Dict[tuple, int] = {}
+        # idle programs per (circuit shape, dtype); one is taken out while its
+        # request is on the device, so a shape may have several
+        self.programs: Dict[tuple, List[int]] = collections.defaultdict(list)
+        self.all_programs: List[int] = []
         self.stats = collections.Counter()
 
     def close(self):
-        for p in self.programs.values():
+        for s in self.streams:
+            self.lib.qgb_stream_sync(s)
+        for p in self.all_programs:
             self.lib.qgb_program_destroy(p)
         for s, e, b in zip(self.streams, self.events, self.batch_ctx):
             self.lib.qgb_stream_sync(s)
@@ -302,7 +310,12 @@ class Server:
             it.nops = len(r.ops)
             it.ops = _op_ptr(r.ops)
             it.coefs = r.coefs.ctypes.data_as(_lib.dp)
-            it.init_zero = 1
+            if r.initial is None:
+                it.init_zero = 1
+            else:
+                init = np.ascontiguousarray(r.initial, dtype=r.dtype)
+                check(self.lib.qgb_memcpy_h2d(st, init.ctypes.data, init.nbytes, stream))
+                it.init_zero = 0
             it.out_kind = OUT_KINDS[r.output]
             it.nshots = r.nshots
             it.seed = r.seed
@@ -337,7 +350,11 @@ class Server:
         st = self.pool.acquire(fp)
         fl.buffers.append((st, fp))
         n = r.nqubits
-        check(self.lib.qgb_state_zero(st, n, code, stream))
+        if r.initial is None:
+            check(self.lib.qgb_state_zero(st, n, code, stream))
+        else:
+            init = np.ascontiguousarray(r.initial, dtype=r.dtype)
+            check(self.lib.qgb_memcpy_h2d(st, init.ctypes.data, init.nbytes, stream))
         if self.one_at_a_time:  # the plain per-gate path: one kernel per gate, IEEE FP64 for complex128
             check(self.lib.qgb_apply_circuit(st, n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
                                              _lib.QGB_PLAN_STRICT_FP64, stream))
@@ -346,20 +363,22 @@ class Server:
                                              _lib.QGB_PLAN_BLOCKED | _lib.QGB_PLAN_FUSE, stream))
             self.stats["fused"] += 1
         else:
-            key = (r.shape, r.dtype, slot)
-            prog = self.programs.get(key)
-            if prog is None:
+            key = (r.shape, r.dtype)
+            if self.programs[key]:
+                prog = self.programs[key].pop()
+                check(self.lib.qgb_program_update(prog, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
+                                                  stream))
+                self.stats["graph_replays"] += 1
+            else:
                 p = C.c_void_p()
                 flags = 0 if self.use_graphs else _lib.QGB_PROGRAM_NO_GRAPH
                 check(self.lib.qgb_program_create(n, code, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
                                                   flags, C.byref(p)))
-                prog = self.programs[key] = p.value
+                prog = p.value
+                self.all_programs.append(prog)
                 self.stats["programs_built"] += 1
-            else:
-                check(self.lib.qgb_program_update(prog, _op_ptr(r.ops), len(r.ops), r.coefs.ctypes.data_as(_lib.dp),
-                                                  stream))
-                self.stats["graph_replays"] += 1
             check(self.lib.qgb_program_run(prog, st, stream))
+            fl.program = (key, prog)
         lay = r.layout()
         if r.output == "shots":
             probs, cdf, samples = st + lay["probs"], st + lay["cdf"], st + lay["out"]
@@ -392,6 +411,9 @@ class Server:
             r.t_done = now
         for p, nbytes in fl.buffers:
             self.pool.release(p, nbytes)
+        if fl.program is not None:
+            key, prog = fl.program
+            self.programs[key].append(prog)
         self.free_slots.append(fl.slot)
 
     # -- the loop -----------------------------------------------------------

@@ -195,3 +195,78 @@ def test_fused_large_requests_concurrent_vs_oracle():
         d, ang = angs[r.rid]
         want = oracle_state(r.nqubits, d, ang, "complex128")
         assert np.max(np.abs(r.result - want)) < TOL[r.dtype] * (10 if r.dtype == "complex64" else 1), (r.rid, r.dtype)
+
+
+def _mixed_circuits(dtype):
+    """Circuits of 6 (batched), 14 (graph-captured program) and 17 qubits
+    (engine fusion), with and without measurements."""
+    from qibo_gb300 import Circuit, gates
+
+    out = []
+    for k, n in enumerate((6, 14, 17, 14, 6)):
+        ops = ref.brickwork_ops(n, 5, 900 + k)
+        c = Circuit(n)
+        for nm, q, p in ops:
+            c.add(getattr(gates, nm)(*q, *p))
+        if k % 2:
+            c.add(gates.M(0, n - 1))
+        out.append(c)
+    return out
+
+
+def test_execute_circuits_on_the_server_equal_alone():
+    """Backend.execute_circuits (backends/abstract.py:2514-2530) through the
+    server: each result equals execute_circuit of that circuit alone; an
+    initial state per circuit is honoured; measured circuits give
+    frequencies over nshots."""
+    from qibo_gb300.backend import GB300Backend
+
+    for dtype in ("complex128", "complex64"):
+        b = GB300Backend(dtype)
+        circs = _mixed_circuits(dtype)
+        rng = np.random.default_rng(4)
+        states = []
+        for c in circs:
+            s = rng.normal(size=2**c.nqubits) + 1j * rng.normal(size=2**c.nqubits)
+            states.append(s / np.linalg.norm(s))
+        for init in (None, states):
+            res = b.execute_circuits(circs, init, nshots=500)
+            st = b.server().stats
+            assert st.get("batched_requests", 0) >= 2 and st.get("fused", 0) >= 1 and st.get("large", 0) >= 3
+            for i, (c, r) in enumerate(zip(circs, res)):
+                alone = b.execute_circuit(c.copy(deep=True), None if init is None else init[i].copy(), nshots=500)
+                got, want = np.asarray(r.state()), np.asarray(alone.state())
+                assert np.max(np.abs(got - want)) < TOL[dtype], (dtype, i, init is None)
+                if c.measurements:
+                    assert sum(r.frequencies().values()) == 500
+
+
+def test_parametrized_sweep_replays_one_graph():
+    """parallel_parametrized_execution (parallel.py:124-192): a 14-qubit
+    RY/CZ circuit with 24 parameter sets runs as requests of one gate shape,
+    which replay the captured graph of that shape; every state equals the
+    circuit run alone with those parameters."""
+    from qibo_gb300 import Circuit, gates
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.parallel import parallel_parametrized_execution
+
+    n = 14
+    b = GB300Backend("complex128")
+    c = Circuit(n)
+    for layer in range(3):
+        c.add([gates.RY(q, theta=0.0) for q in range(n)])
+        c.add([gates.CZ(q, q + 1) for q in range(layer % 2, n - 1, 2)])
+    c.add([gates.RY(q, theta=0.0) for q in range(n)])
+    nparams = len(c.get_parameters())
+    rng = np.random.default_rng(8)
+    params = [rng.uniform(0, 2 * np.pi, nparams) for _ in range(24)]
+    res = parallel_parametrized_execution(c, params, backend=b)
+    st = b.server().stats
+    assert st.get("graph_replays", 0) >= 24 - 8 and st.get("programs_built", 0) <= 8, dict(st)
+    for p, r in zip(params, res):
+        one = c.copy(deep=True)
+        one.set_parameters(p)
+        want = np.asarray(b.execute_circuit(one).state())
+        assert np.max(np.abs(np.asarray(r.state()) - want)) < TOL["complex128"]
+    # the template circuit's own parameters are left alone
+    assert all(abs(v[0]) == 0.0 for v in c.get_parameters())
