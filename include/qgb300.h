@@ -249,6 +249,41 @@ size_t qgb_expect_scratch_bytes(int nqubits, int nterms);
 int qgb_expect_dense(const void* state, int nqubits, int dtype, const double* hamiltonian, double* out,
                      void* scratch, void* stream);
 
+/* ---- density matrices ------------------------------------------------------
+ * A density matrix rho of n qubits (n <= 20) is the 2n-qubit "state"
+ * v[i * 2^n + j] = rho[i, j] (row-major, the reference's rho.ravel()): row
+ * qubit q is vector qubit q, column qubit q is vector qubit n + q.  A gate U
+ * on qubits T is qgb_apply_circuit of U on T and conj(U) on T + n (the two
+ * einsums of Backend.apply_gate with a density matrix,
+ * backends/abstract.py:2322-2361, and _apply_gate_controlled_by_density_
+ * matrix, :3199-3247, with the controls shifted likewise); a channel on T is
+ * one dense superoperator on (T, T + n).  ``nqubits`` below is n. */
+/* out[0..2^nq) (device, FP64) = marginal probabilities of ``qubits`` from
+ * the diagonal (Backend.calculate_probabilities with density_matrix=True,
+ * backends/abstract.py:2734-2758), qubits[0] the most significant outcome
+ * bit; nq = 0 gives the real trace.  Fixed reduction order. */
+size_t qgb_density_scratch_bytes(void);
+int qgb_density_probabilities(const void* rho, int nqubits, int dtype, const int* qubits, int nq, double* out,
+                              void* scratch, void* stream);
+/* Backend.collapse_state with density_matrix=True (_collapse_density_matrix,
+ * backends/abstract.py:3249-3277): entries whose row or column bits on
+ * ``qubits`` differ from outcome *outcome (device int64) become 0; with
+ * ``normalize`` the kept block is divided by its real trace.  ``scratch``:
+ * qgb_density_scratch_bytes() bytes. */
+int qgb_density_collapse(void* rho, int nqubits, int dtype, const int* qubits, int nq, const int64_t* outcome,
+                         int normalize, void* scratch, void* stream);
+/* out (device, FP64) = sum_t coef[t] Re Tr(P_t rho), Pauli strings as in
+ * qgb_expect_pauli (Backend.exp_value_observable_symbolic on a density
+ * matrix, backends/abstract.py:2975-3054).  ``scratch``:
+ * qgb_density_scratch_bytes() bytes. */
+int qgb_density_expect_pauli(const void* rho, int nqubits, int dtype, const uint64_t* xmask, const uint64_t* zmask,
+                             const double* coef, int nterms, double* out, void* scratch, void* stream);
+/* y = a x + b y over 2^nqubits amplitudes (b = 0: y is only written): the
+ * weighted sum of Backend.apply_channel (backends/abstract.py:2297-2312) for
+ * channels wider than one superoperator, and the mean of the final density
+ * matrices of repeated execution (:2603-2607). */
+int qgb_state_axpby(void* y, const void* x, int nqubits, int dtype, double a, double b, void* stream);
+
 /* ---- gradients: the reference has parameter shift and finite differences
  *      only (derivative.py:7-226); these implement the adjoint method ----- */
 /* dst = sum_t coef[t] P_t src for Pauli strings given as qubit bit masks

@@ -519,3 +519,256 @@ def parameter_shift_grad(build_ops, nqubits, params, terms, term_qubits, coeffs,
         em = energy(p)
         grads[i] = eig * (ep - em) * scale_factor
     return grads
+
+
+# --------------------------------------------------------------------------
+# Density matrices: backends/abstract.py:2095-2241, :2297-2361, :2734-2748,
+# :2807-2816, :2975-3054, :3199-3277
+# --------------------------------------------------------------------------
+
+def apply_gate_density(rho: np.ndarray, matrix: np.ndarray, qubits: Sequence[int], nqubits: int) -> np.ndarray:
+    """``Backend.apply_gate`` density branch (:2339-2349) with
+    ``einsum_utils.apply_gate_density_matrix_string``
+    (backends/einsum_utils.py:36-44): conj(U) contracted into the column
+    axes ("right" string), then U into the row axes ("left" string)."""
+    n, k = nqubits, len(qubits)
+    m = np.reshape(matrix, 2 * k * (2,))
+    inp = list(ascii_letters[:n])
+    out = list(inp)
+    trans = list(ascii_letters[n:n + k])
+    for i, q in enumerate(qubits):
+        trans.append(inp[q])
+        out[q] = trans[i]
+    rest = ascii_letters[n + k:n + k + n]
+    inp, out, trans = "".join(inp), "".join(out), "".join(trans)
+    st = np.reshape(rho, 2 * n * (2,))
+    st = np.einsum(f"{rest}{inp},{trans}->{rest}{out}", st, np.conj(m))
+    st = np.einsum(f"{inp}{rest},{trans}->{out}{rest}", st, m)
+    return np.reshape(st, (2**n, 2**n))
+
+
+def controlled_matrix(matrix: np.ndarray, ncontrols: int) -> np.ndarray:
+    """U with ``ncontrols`` controls as one matrix on controls + targets: the
+    identity except the all-ones control block."""
+    d = matrix.shape[0] * 2**ncontrols
+    full = np.eye(d, dtype=np.complex128)
+    full[d - matrix.shape[0]:, d - matrix.shape[0]:] = matrix
+    return full
+
+
+def apply_gate_controlled_by_density(rho, matrix, controls, targets, nqubits) -> np.ndarray:
+    """``Backend._apply_gate_controlled_by_density_matrix`` (:3199-3234)
+    computes V rho V^dagger for V = U controlled on ``controls`` block by
+    block; here V is formed and applied whole (the same map)."""
+    return apply_gate_density(rho, controlled_matrix(matrix, len(controls)), list(sorted(controls)) + list(targets),
+                              nqubits)
+
+
+def apply_channel_density(rho: np.ndarray, coefficients, gates, coefficient_sum, nqubits: int) -> np.ndarray:
+    """``Backend.apply_channel`` density branch (:2304-2312):
+    (1 - sum c) rho + sum_k c_k K_k rho K_k^dagger; ``gates`` are
+    (qubits, matrix) pairs."""
+    new = (1 - coefficient_sum) * rho
+    for c, (qs, m) in zip(coefficients, gates):
+        new = new + c * apply_gate_density(rho, m, qs, nqubits)
+    return new
+
+
+def partial_trace_keep(rho: np.ndarray, traced: Sequence[int], nqubits: int) -> np.ndarray:
+    """Tr over ``traced`` qubits, the others kept in ascending order."""
+    keep = [q for q in range(nqubits) if q not in traced]
+    st = np.reshape(rho, 2 * nqubits * (2,))
+    inp = list(ascii_letters[:2 * nqubits])
+    for q in traced:
+        inp[q + nqubits] = inp[q]
+    outs = "".join(inp[q] for q in keep) + "".join(inp[q + nqubits] for q in keep)
+    red = np.einsum("".join(inp) + "->" + outs, st)
+    d = 2 ** len(keep)
+    return np.reshape(red, (d, d))
+
+
+def _with_factor(reduced: np.ndarray, factor: np.ndarray, qubits: Sequence[int], nqubits: int) -> np.ndarray:
+    """reduced (on the qubits not in ``qubits``, ascending) (x) factor (on
+    ``qubits`` in that order), axes put back in qubit order."""
+    keep = [q for q in range(nqubits) if q not in qubits]
+    t = np.tensordot(np.reshape(reduced, 2 * len(keep) * (2,)), np.reshape(factor, 2 * len(qubits) * (2,)), 0)
+    # t's axes: kept rows, kept columns, factor rows, factor columns
+    axes = keep + [q + nqubits for q in keep] + list(qubits) + [q + nqubits for q in qubits]
+    perm = [axes.index(a) for a in range(2 * nqubits)]
+    return np.reshape(np.transpose(t, perm), (2**nqubits, 2**nqubits))
+
+
+def depolarizing_density(rho: np.ndarray, qubits: Sequence[int], lam: float, nqubits: int) -> np.ndarray:
+    """``Backend.depolarizing_error_density_matrix`` (:2095-2132):
+    (1 - lam) rho + lam Tr_T(rho) (x) I / 2^|T|."""
+    d = 2 ** len(qubits)
+    mixed = _with_factor(partial_trace_keep(rho, qubits, nqubits), np.eye(d) / d, qubits, nqubits)
+    return (1 - lam) * rho + lam * mixed
+
+
+def reset_density(rho: np.ndarray, qubit: int, p0: float, p1: float, nqubits: int) -> np.ndarray:
+    """``Backend.reset_error_density_matrix`` (:2212-2232):
+    (1 - p0 - p1) rho + p0 Tr_q(rho) (x) |0><0| + p1 X_q (that) X_q."""
+    zero = _with_factor(partial_trace_keep(rho, [qubit], nqubits), np.diag([1.0, 0.0]), [qubit], nqubits)
+    x = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+    return (1 - p0 - p1) * rho + p0 * zero + p1 * apply_gate_density(zero, x, [qubit], nqubits)
+
+
+def thermal_density(rho: np.ndarray, qubit: int, t_1: float, t_2: float, kw: dict, nqubits: int) -> np.ndarray:
+    """``ThermalRelaxationChannel.apply`` (gates/channels.py:678-707): for
+    T1 < T2 a 4 x 4 matrix on (q, q + n) of the flattened density matrix
+    (thermal_error_density_matrix, :2234-2241); otherwise the reset map
+    minus p_z rho plus p_z Z rho Z with Z on qubit 0, as the reference
+    writes it (gates/channels.py:702-706)."""
+    p0, p1 = kw["p_0"], kw["p_1"]
+    if t_1 < t_2:
+        e = kw["e_t2"]
+        m = np.array([[1 - p1, 0, 0, p0], [0, e, 0, 0], [0, 0, e, 0], [p1, 0, 0, 1 - p0]], dtype=np.complex128)
+        v = apply_gate(np.ravel(rho), m, [qubit, qubit + nqubits], 2 * nqubits)
+        return np.reshape(v, rho.shape)
+    pz = kw["p_z"]
+    z = np.diag([1.0, -1.0]).astype(np.complex128)
+    return reset_density(rho, qubit, p0, p1, nqubits) - pz * rho + pz * apply_gate_density(rho, z, [0], nqubits)
+
+
+def calculate_probabilities_density(rho: np.ndarray, qubits: Sequence[int], nqubits: int) -> np.ndarray:
+    """``Backend.calculate_probabilities`` density branch (:2741-2748):
+    measured qubits (sorted) to the front on both sides, "abab->a", then
+    ``_order_probabilities``."""
+    order = tuple(sorted(qubits))
+    order += tuple(q for q in range(nqubits) if q not in qubits)
+    order = order + tuple(q + nqubits for q in order)
+    shape = 2 * (2 ** len(qubits), 2 ** (nqubits - len(qubits)))
+    st = np.reshape(np.transpose(np.reshape(rho, 2 * nqubits * (2,)), order), shape)
+    probs = np.abs(np.einsum("abab->a", st))
+    probs = np.reshape(probs, len(qubits) * (2,))
+    return order_probabilities(probs, qubits, nqubits).ravel()
+
+
+def collapse_density(rho: np.ndarray, qubits: Sequence[int], shot: int, nqubits: int,
+                     normalize: bool = True) -> np.ndarray:
+    """``Backend._collapse_density_matrix`` (:3249-3277): the block of
+    outcome ``shot`` on rows and columns, divided by its trace, with zeros
+    elsewhere."""
+    qubits = list(qubits)
+    binshot = list(samples_to_binary(np.array([shot], dtype=np.int64), len(qubits))[0])
+    order = qubits + [q + nqubits for q in qubits]
+    order += [q for q in range(nqubits) if q not in qubits]
+    order += [q + nqubits for q in range(nqubits) if q not in qubits]
+    st = np.transpose(np.reshape(rho, 2 * nqubits * (2,)), order)
+    sub = 2 * (2 ** len(qubits),) + 2 * (nqubits - len(qubits)) * (2,)
+    st = np.reshape(st, sub)[int(shot), int(shot)]
+    if normalize:
+        dims = 2 ** (len(st.shape) // 2)
+        st = st / np.trace(np.reshape(st, (dims, dims)))
+    for q, r in zip(qubits + [q + nqubits for q in qubits], 2 * binshot):
+        st = np.expand_dims(st, q)
+        st = np.concatenate([np.zeros_like(st), st], axis=q) if r == 1 else np.concatenate([st, np.zeros_like(st)], axis=q)
+    return np.reshape(st, rho.shape)
+
+
+_PAULI = {"X": np.array([[0, 1], [1, 0]], dtype=np.complex128), "Y": np.array([[0, -1j], [1j, 0]]),
+          "Z": np.array([[1, 0], [0, -1]], dtype=np.complex128), "I": np.eye(2, dtype=np.complex128)}
+
+
+def exp_value_observable_symbolic_density(rho, terms: Sequence[str], term_qubits, term_coefficients,
+                                          nqubits: int) -> float:
+    """``Backend.exp_value_observable_symbolic`` density branch
+    (:3009-3030): per term, Re(c Tr(P rho)) contracted factor by factor."""
+    total = 0.0
+    for term, qubits, c in zip(terms, term_qubits, term_coefficients):
+        st = np.array(rho, dtype=np.complex128)
+        for f, q in zip(term, qubits):
+            if f != "I":
+                st = np.reshape(apply_gate(np.ravel(st), _PAULI[f], [q], 2 * nqubits), st.shape)  # P acting on rows
+        total += float(np.real(c * np.trace(st)))
+    return total
+
+
+def expectation_value_density(hamiltonian: np.ndarray, rho: np.ndarray, normalize: bool) -> float:
+    """``Backend.expectation_value`` density branch (:2810-2816)."""
+    ev = float(np.real(np.trace(hamiltonian @ rho)))
+    if normalize:
+        ev /= float(np.real(np.trace(rho)))
+    return ev
+
+
+def thermal_parameters(t_1: float, t_2: float, time: float, excited_population: float = 0.0) -> dict:
+    """``ThermalRelaxationChannel.__init__`` (gates/channels.py:601-660):
+    p_0 = (1 - e^(-t/T1)) (1 - eta), p_1 = (1 - e^(-t/T1)) eta, and e_t2 =
+    e^(-t/T2) for T1 < T2, else p_z = (e^(-t/T1) - e^(-t/T2)) / 2."""
+    p_reset = 1 - math.exp(-time / t_1)
+    kw = {"p_0": p_reset * (1 - excited_population), "p_1": p_reset * excited_population}
+    if t_1 < t_2:
+        kw["e_t2"] = math.exp(-time / t_2)
+    else:
+        kw["p_z"] = (math.exp(-time / t_1) - math.exp(-time / t_2)) / 2
+    return kw
+
+
+_NQ = {"H": 1, "X": 1, "Y": 1, "Z": 1, "RX": 1, "RY": 1, "RZ": 1, "U3": 1, "CNOT": 2, "CZ": 2, "fSim": 2,
+       "SWAP": 2, "TOFFOLI": 3}
+
+
+def _pauli_string(s: str) -> np.ndarray:
+    m = np.eye(1, dtype=np.complex128)
+    for f in s:
+        m = np.kron(m, _PAULI[f])
+    return m
+
+
+def execute_density(ops, nqubits: int, rho=None) -> np.ndarray:
+    """A density-matrix circuit given as (gate or channel name, constructor
+    arguments, controlled_by qubits) in the reference's constructor
+    conventions (gates/gates.py, gates/channels.py), applied as the
+    reference's NumpyBackend does: gates by ``apply_gate_density``, Kraus /
+    unitary / Pauli / amplitude- and phase-damping / readout channels by
+    ``apply_channel_density``, depolarizing, reset and thermal relaxation by
+    their special forms."""
+    n = nqubits
+    if rho is None:
+        rho = np.zeros((2**n, 2**n), dtype=np.complex128)
+        rho[0, 0] = 1
+    rho = np.array(rho, dtype=np.complex128)
+    for name, args, controls in ops:
+        if name == "DepolarizingChannel":
+            qs = (args[0],) if isinstance(args[0], int) else tuple(args[0])
+            rho = depolarizing_density(rho, qs, args[1], n)
+        elif name == "ResetChannel":
+            rho = reset_density(rho, args[0], args[1][0], args[1][1], n)
+        elif name == "ThermalRelaxationChannel":
+            p = list(args[1])
+            rho = thermal_density(rho, args[0], p[0], p[1], thermal_parameters(*p), n)
+        elif name == "PauliNoiseChannel":
+            qs = (args[0],) if isinstance(args[0], int) else tuple(args[0])
+            probs = [pr for _, pr in args[1]]
+            rho = apply_channel_density(rho, probs, [(qs, _pauli_string(s)) for s, _ in args[1]], sum(probs), n)
+        elif name in ("AmplitudeDampingChannel", "PhaseDampingChannel"):
+            g = args[1]
+            k1 = [[0, math.sqrt(g)], [0, 0]] if name == "AmplitudeDampingChannel" else [[0, 0], [0, math.sqrt(g)]]
+            ks = [np.array([[1, 0], [0, math.sqrt(1 - g)]], dtype=np.complex128), np.array(k1, dtype=np.complex128)]
+            rho = apply_channel_density(rho, [1, 1], [((args[0],), k) for k in ks], 1, n)
+        elif name == "ReadoutErrorChannel":
+            P = np.asarray(args[1])
+            qs = (args[0],) if isinstance(args[0], int) else tuple(args[0])
+            ks = []
+            for j in range(len(P)):
+                for k in range(len(P)):
+                    m = np.zeros((len(P), len(P)), dtype=np.complex128)
+                    m[j, k] = math.sqrt(P[k, j])
+                    ks.append((qs, m))
+            rho = apply_channel_density(rho, [1] * len(ks), ks, 1, n)
+        elif name == "KrausChannel":
+            rho = apply_channel_density(rho, [1] * len(args[1]), list(zip(args[0], args[1])), 1, n)
+        elif name == "UnitaryChannel":
+            probs = [p for p, _ in args[1]]
+            rho = apply_channel_density(rho, probs, list(zip(args[0], [u for _, u in args[1]])), sum(probs), n)
+        else:
+            k = _NQ[name]
+            qs, params = tuple(args[:k]), tuple(args[k:])
+            m = gate_matrix(name, params)
+            if controls:
+                rho = apply_gate_controlled_by_density(rho, m, controls, qs, n)
+            else:
+                rho = apply_gate_density(rho, m, qs, n)
+    return rho

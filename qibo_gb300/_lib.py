@@ -97,6 +97,11 @@ SIGNATURES = {
     "qgb_inner_scratch_bytes": (sz, []),
     "qgb_inner": (i32, [vp, vp, i32, i32, vp, vp, vp]),
     "qgb_inner_mixed": (i32, [vp, i32, vp, i32, i32, vp, vp, vp]),
+    "qgb_density_scratch_bytes": (sz, []),
+    "qgb_density_probabilities": (i32, [vp, i32, i32, ip, i32, vp, vp, vp]),
+    "qgb_density_collapse": (i32, [vp, i32, i32, ip, i32, vp, i32, vp, vp]),
+    "qgb_density_expect_pauli": (i32, [vp, i32, i32, u64p, u64p, dp, i32, vp, vp, vp]),
+    "qgb_state_axpby": (i32, [vp, vp, i32, i32, f64, f64, vp]),
     "qgb_adjoint_scratch_bytes": (sz, [i32]),
     "qgb_adjoint_sweep": (i32, [vp, vp, i32, i32, C.POINTER(QgbOp), i32, dp, ip, C.POINTER(C.c_int64), ip, i32,
                                 vp, vp, vp]),

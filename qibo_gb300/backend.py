@@ -41,7 +41,8 @@ import numpy as np
 from . import _lib
 from . import gates as G
 from ._lib import DeviceOutOfMemory, check, int_array
-from .device import DeviceArray, DeviceState, Runtime
+from .density import compile_queue, gate_pair, is_channel, wide_terms
+from .device import DeviceArray, DeviceDensity, DeviceState, Runtime
 from .engine import Engine, pauli_masks
 
 SKIP_GATES = ("M", "I", "Align", "CallbackGate")
@@ -56,8 +57,8 @@ def describe_gate(gate, backend):
         if name == "M" and getattr(gate, "collapse", False):
             raise NotImplementedError("collapsing measurements are not supported by qibo_gb300")
         return None
-    if name.endswith("Channel") or name in ("KrausChannel", "UnitaryChannel", "PauliNoiseChannel"):
-        raise NotImplementedError("noise channels need the density-matrix path, not supported")
+    if is_channel(gate):
+        raise NotImplementedError(f"{name} cannot be applied to statevector.")
     m = np.asarray(gate.matrix(backend), dtype=np.complex128)
     if getattr(gate, "is_controlled_by", False):
         return tuple(gate.target_qubits), tuple(gate.control_qubits), m
@@ -96,9 +97,9 @@ class GB300Methods:
 
     # -- states -----------------------------------------------------------
     def zero_state(self, nqubits, density_matrix=False, dtype=None):
+        self._validate_nqubits(nqubits, density_matrix=density_matrix)
         if density_matrix:
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
-        self._validate_nqubits(nqubits)
+            return DeviceDensity.zero(nqubits, dtype or self.dtype)
         return DeviceState.zero(nqubits, dtype or self.dtype)
 
     def cast(self, array, dtype=None, copy=False):
@@ -116,9 +117,9 @@ class GB300Methods:
         if isinstance(state, DeviceState):
             return state
         arr = np.asarray(state)
-        if arr.ndim != 1:
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
         dt = dtype or (arr.dtype if arr.dtype in (np.complex64, np.complex128) else self.dtype)
+        if arr.ndim == 2:
+            return DeviceDensity.from_numpy(arr, dt)
         return DeviceState.from_numpy(arr, dt)
 
     # -- gates ------------------------------------------------------------
@@ -126,6 +127,9 @@ class GB300Methods:
         """In place on the device state (qibojit's convention,
         doc/source/getting-started/backends.rst:57-61); returns the state."""
         state = self._as_device_state(state)
+        if isinstance(state, DeviceDensity):
+            self._run_density(state, compile_queue([gate], self, state.nsys, self._describe))
+            return state
         desc = describe_gate(gate, self)
         if desc is not None:
             if self.dtype == "complex128" and not self.strict_fp64:
@@ -140,10 +144,123 @@ class GB300Methods:
     def matrix_fused(self, fgate):
         return G.fused_matrix(fgate.target_qubits, fgate.gates, self)
 
+    def _describe(self, gate):
+        return describe_gate(gate, self)
+
+    # -- density matrices and channels ----------------------------------------
+    def apply_channel(self, channel, state, nqubits):
+        """Backend.apply_channel (backends/abstract.py:2297-2318).  On a
+        density matrix: the channel's superoperator on the device, in place.
+        On a state vector: one of the channel's gates, or none, drawn with
+        the channel's probabilities by the device sampler and applied."""
+        state = self._as_device_state(state)
+        if isinstance(state, DeviceDensity):
+            self._run_density(state, compile_queue([channel], self, state.nsys, self._describe))
+            return state
+        probs = [float(np.real(c)) for c in channel.coefficients]
+        probs.append(max(0.0, 1.0 - sum(probs)))
+        index = int(self.sample_shots(np.asarray(probs), 1)[0])
+        if index != len(channel.gates):
+            state = self.apply_gate(channel.gates[index], state, nqubits)
+        return state
+
+    def depolarizing_error_density_matrix(self, gate, state, nqubits):
+        """backends/abstract.py:2095-2132, in place on the device."""
+        return self.apply_channel(gate, state, nqubits)
+
+    def reset_error_density_matrix(self, gate, state, nqubits):
+        """backends/abstract.py:2212-2232: the reset map of ``gate``'s p_0 and
+        p_1 on its qubit, into a new density matrix (the caller may combine
+        it with the input, as ThermalRelaxationChannel.apply does)."""
+        from .density import _reset_superop
+
+        rho = self._as_device_state(state).copy()
+        q = gate.target_qubits[0]
+        kw = gate.init_kwargs
+        n = rho.nsys
+        self._run_density(rho, [("gates", [((q, q + n), (), _reset_superop(float(kw["p_0"]), float(kw["p_1"])))])])
+        return rho
+
+    def thermal_error_density_matrix(self, gate, state, nqubits):
+        """backends/abstract.py:2234-2241: ``gate`` acts on (q, q + n) of the
+        2n-qubit vector of the density matrix, in place."""
+        rho = self._as_device_state(state)
+        m = np.asarray(gate.matrix(self), dtype=np.complex128)
+        self._run_density(rho, [("gates", [(tuple(gate.qubits), (), m)])])
+        return rho
+
+    def _run_density(self, rho, items):
+        """Run compiled density items (qibo_gb300.density.compile_queue) on ``rho``."""
+        fuse = self.blocked and self.fuse and rho.nqubits >= FUSE_MIN_QUBITS
+        for kind, payload in items:
+            if kind == "gates":
+                self.engine_gb.apply_many(rho, payload, blocked=self.blocked, strict_fp64=self.strict_fp64, fuse=fuse)
+            elif kind == "wide":
+                self._apply_wide_channel(rho, payload)
+            else:
+                raise RuntimeError("collapsing measurements on density matrices run through repeated execution")
+
+    def _apply_wide_channel(self, rho, channel):
+        """A channel whose superoperator exceeds a 5-qubit gate, as the
+        reference's weighted sum (backends/abstract.py:2305-2310): each term
+        on a copy of rho, accumulated on the device."""
+        keep, terms = wide_terms(channel, self, rho.nsys)
+        eng, lib, s = self.engine_gb, self.rt.lib, self.rt.stream
+        acc = DeviceDensity(rho.nsys, rho.dtype, self.rt)
+        work = DeviceDensity(rho.nsys, rho.dtype, self.rt)
+        eng.axpby(acc, rho, keep, 0.0)
+        fuse = self.blocked and self.fuse and rho.nqubits >= FUSE_MIN_QUBITS
+        for c, pair in terms:
+            check(lib.qgb_memcpy_d2d(work.ptr, rho.ptr, rho.nbytes, s))
+            eng.apply_many(work, pair, blocked=self.blocked, strict_fp64=self.strict_fp64, fuse=fuse)
+            eng.axpby(acc, work, c, 1.0)
+        check(lib.qgb_memcpy_d2d(rho.ptr, acc.ptr, rho.nbytes, s))
+
+    def _initial_density(self, initial_state, nqubits):
+        if initial_state is None:
+            return DeviceDensity.zero(nqubits, self.dtype)
+        shape = tuple(initial_state.shape)
+        if shape != (2**nqubits, 2**nqubits):
+            raise ValueError(f"Given initial state has shape {shape} instead of the expected "
+                             f"{(2 ** nqubits, 2 ** nqubits)}.")
+        if isinstance(initial_state, DeviceDensity):
+            return initial_state  # in place, like qibojit
+        return self._as_device_state(initial_state)
+
+    def _execute_density(self, circuit, initial_state, nshots):
+        """execute_circuit for ``density_matrix=True`` circuits
+        (backends/abstract.py:2442-2512 and _execute_circuit, :3306-3345):
+        gates and channels as 2n-qubit operations on the device (see
+        qibo_gb300.density), collapsing measurements through repeated
+        execution."""
+        nqubits = circuit.nqubits
+        self._validate_nqubits(nqubits, density_matrix=True)
+        if initial_state is not None and hasattr(initial_state, "queue") and hasattr(initial_state, "nqubits"):
+            if not getattr(initial_state, "density_matrix", False):
+                raise ValueError("Cannot set circuit with density_matrix False as initial state for circuit with "
+                                 "density_matrix True.")
+            return self.execute_circuit(initial_state + circuit, None, nshots)
+        if getattr(circuit, "repeated_execution", False):
+            return self.execute_circuit_repeated(circuit, nshots, initial_state)
+        try:
+            rho = self._initial_density(initial_state, nqubits)
+            self._run_density(rho, compile_queue(circuit.queue, self, nqubits, self._describe))
+        except DeviceOutOfMemory:
+            raise RuntimeError(f"State does not fit in {self.device} memory."
+                               "Please switch the execution device to a "
+                               "different one using ``qibo.set_device``.")
+        QuantumState, CircuitResult = self._result_classes()
+        if circuit.measurements:
+            result = CircuitResult(rho, circuit.measurements, backend=self, nshots=nshots)
+        else:
+            result = QuantumState(rho, backend=self)
+        circuit._final_state = result
+        return result
+
     def execute_circuit(self, circuit, initial_state=None, nshots=1000):
         nqubits = circuit.nqubits
         if getattr(circuit, "density_matrix", False):
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
+            return self._execute_density(circuit, initial_state, nshots)
         self._validate_nqubits(nqubits)
         if getattr(circuit, "repeated_execution", False):
             if not circuit.measurements and not getattr(circuit, "has_collapse", False):
@@ -207,53 +324,93 @@ class GB300Methods:
 
     def execute_circuit_repeated(self, circuit, nshots, initial_state=None):
         """Backend.execute_circuit_repeated (backends/abstract.py:2532-2636)
-        for circuits with collapsing measurements, on the device.  Every shot
-        runs the circuit again from the initial state.  A collapsing
-        measurement draws its outcome on the device from the FP64
-        probabilities of its sorted qubits (as gates/measurements.py:199-204),
-        and ``qgb_collapse`` projects the state onto it straight from device
-        memory.  The final measurements draw one shot each into a device
-        array.  The host only queues launches, and the outcomes come back
-        once, after the last shot."""
-        if getattr(circuit, "has_unitary_channel", False):
-            raise NotImplementedError("noisy repeated execution needs noise channels, not supported by qibo_gb300")
-        if getattr(circuit, "has_collapse", False) and not circuit.measurements:
+        on the device, for circuits with collapsing measurements and for
+        noisy state-vector circuits.  Every shot runs the circuit again from
+        the initial state.  A collapsing measurement draws its outcome on the
+        device from the FP64 probabilities of its sorted qubits (as
+        gates/measurements.py:199-218), and the collapse reads it straight
+        from device memory.  A unitary channel on a state vector applies one
+        of its gates per shot, drawn for all shots at once by the device
+        sampler (Backend.apply_channel, :2314-2318).  The final measurements
+        draw one shot each into a device array.  Density-matrix circuits
+        return the mean of the shots' final density matrices, accumulated on
+        the device (:2603-2625)."""
+        density = bool(getattr(circuit, "density_matrix", False))
+        if getattr(circuit, "has_collapse", False) and not circuit.measurements and not density:
             raise RuntimeError("The circuit contains only collapsing measurements (`collapse=True`) but "
                                "`density_matrix=False`. Please set `density_matrix=True` to retrieve the final "
                                "state after execution.")
         nqubits, nshots = circuit.nqubits, int(nshots)
+        nvec = 2 * nqubits if density else nqubits
         eng, rt, lib = self.engine_gb, self.rt, self.rt.lib
         flags = ((_lib.QGB_PLAN_BLOCKED if self.blocked else 0) | (_lib.QGB_PLAN_STRICT_FP64 if self.strict_fp64 else 0)
-                 | (_lib.QGB_PLAN_FUSE if self.blocked and self.fuse and nqubits >= FUSE_MIN_QUBITS else 0))
-        # the circuit as runs of gates (packed once) and collapsing measurements
-        items, run, collapse_gates = [], [], []
+                 | (_lib.QGB_PLAN_FUSE if self.blocked and self.fuse and nvec >= FUSE_MIN_QUBITS else 0))
         for g in circuit.queue:
             if getattr(g, "symbolic_parameters", None):
                 raise NotImplementedError("parameters that depend on measurement outcomes are not supported")
-            if type(g).__name__ == "M":
-                if getattr(g, "collapse", False):
+        # the circuit as items: runs of gates (packed once), collapsing
+        # measurements, channels
+        items, collapse_gates = [], []
+        if density:
+            for kind, payload in compile_queue(circuit.queue, self, nqubits, self._describe):
+                if kind == "gates":
+                    items.append(("gates", eng.pack_ops(payload), len(payload)))
+                elif kind == "wide":
+                    items.append(("wide", payload, 0))
+                else:
+                    qs = sorted(payload.target_qubits)
+                    items.append(("collapse", int_array(qs), len(qs)))
+                    collapse_gates.append((payload, len(qs)))
+        else:
+            run = []
+            for g in circuit.queue:
+                if type(g).__name__ == "M":
+                    if getattr(g, "collapse", False):
+                        if run:
+                            items.append(("gates", eng.pack_ops(run), len(run)))
+                            run = []
+                        qs = sorted(g.target_qubits)
+                        items.append(("collapse", int_array(qs), len(qs)))
+                        collapse_gates.append((g, len(qs)))
+                    continue
+                if is_channel(g):
+                    if not any(c.__name__ == "UnitaryChannel" for c in type(g).__mro__):
+                        raise NotImplementedError(f"{type(g).__name__} cannot be applied to statevector.")
                     if run:
                         items.append(("gates", eng.pack_ops(run), len(run)))
                         run = []
-                    qs = sorted(g.target_qubits)
-                    items.append(("collapse", int_array(qs), len(qs)))
-                    collapse_gates.append((g, len(qs)))
-                continue
-            d = describe_gate(g, self)
-            if d is not None:
-                run.append(d)
-        if run:
-            items.append(("gates", eng.pack_ops(run), len(run)))
+                    opts = []
+                    for x in g.gates:
+                        d = describe_gate(x, self)
+                        opts.append(None if d is None else eng.pack_ops([d]))
+                    probs = [float(np.real(c)) for c in g.coefficients]
+                    probs.append(max(0.0, 1.0 - sum(probs)))
+                    draws = eng.sample(self._device_probs(np.asarray(probs)), nshots, self._next_key(), counts=False)
+                    items.append(("channel", (opts, draws), 0))
+                    continue
+                d = describe_gate(g, self)
+                if d is not None:
+                    run.append(d)
+            if run:
+                items.append(("gates", eng.pack_ops(run), len(run)))
         meas_q = [q for m in circuit.measurements for q in m.target_qubits]
         nmeas, ncol = len(meas_q), len(collapse_gates)
+        if density:
+            probs_call, collapse_call, scratch_sizes = (lib.qgb_density_probabilities, lib.qgb_density_collapse,
+                                                        [lib.qgb_density_scratch_bytes()])
+        else:
+            probs_call, collapse_call = lib.qgb_probabilities, lib.qgb_collapse
+            scratch_sizes = [lib.qgb_norm_scratch_bytes(), lib.qgb_probs_scratch_bytes(nqubits, nmeas)]
+            scratch_sizes += [lib.qgb_probs_scratch_bytes(nqubits, m) for _, m in collapse_gates]
         try:
-            state = DeviceState(nqubits, self.dtype)
+            state = DeviceDensity(nqubits, self.dtype) if density else DeviceState(nqubits, self.dtype)
+            mean = DeviceDensity(nqubits, self.dtype) if density else None
             init = None
             if initial_state is not None:
                 init = self._as_device_state(initial_state)
-                if tuple(init.shape) != (2**nqubits,):
+                if tuple(init.shape) != tuple(state.shape):
                     raise ValueError(f"Given initial state has shape {tuple(init.shape)} instead of the expected "
-                                     f"{(2 ** nqubits,)}.")
+                                     f"{tuple(state.shape)}.")
                 if init.dtype != state.dtype:
                     init = init.astype(state.dtype)
             # device buffers for every shot, allocated once
@@ -261,33 +418,44 @@ class GB300Methods:
             fin_probs = DeviceArray((2**nmeas,), np.float64, rt)
             outcomes = DeviceArray((max(1, nshots * ncol),), np.int64, rt)
             samples = DeviceArray((max(1, nshots),), np.int64, rt)
-            sizes = [lib.qgb_norm_scratch_bytes(), lib.qgb_sample_scratch_bytes(nmeas),
-                     lib.qgb_probs_scratch_bytes(nqubits, nmeas)]
+            sizes = scratch_sizes + [lib.qgb_sample_scratch_bytes(nmeas)]
             sizes += [lib.qgb_sample_scratch_bytes(m) for _, m in collapse_gates]
-            sizes += [lib.qgb_probs_scratch_bytes(nqubits, m) for _, m in collapse_gates]
             scratch = rt.scratch(max(sizes))
             mq = int_array(meas_q)
             code, s = state.code, rt.stream
+            n_probs = nqubits  # the probability and collapse calls take the system size
             for shot in range(nshots):
                 if init is None:
-                    check(lib.qgb_state_zero(state.ptr, nqubits, code, s))
+                    check(lib.qgb_state_zero(state.ptr, nvec, code, s))
                 else:
                     check(lib.qgb_memcpy_d2d(state.ptr, init.ptr, state.nbytes, s))
                 j = 0
                 for kind, payload, k in items:
                     if kind == "gates":
                         ops, allc = payload
-                        check(lib.qgb_apply_circuit(state.ptr, nqubits, code, ops, k, allc.ctypes.data_as(_lib.dp),
+                        check(lib.qgb_apply_circuit(state.ptr, nvec, code, ops, k, allc.ctypes.data_as(_lib.dp),
                                                     flags, s))
+                    elif kind == "channel":
+                        opts, draws = payload
+                        idx = int(draws[shot])
+                        if idx < len(opts) and opts[idx] is not None:
+                            ops, allc = opts[idx]
+                            check(lib.qgb_apply_circuit(state.ptr, nvec, code, ops, 1, allc.ctypes.data_as(_lib.dp),
+                                                        flags, s))
+                    elif kind == "wide":
+                        self._apply_wide_channel(state, payload)
                     else:
                         out = outcomes.ptr + 8 * (shot * ncol + j)
-                        check(lib.qgb_probabilities(state.ptr, nqubits, code, payload, k, col_probs[j].ptr, scratch, s))
+                        check(probs_call(state.ptr, n_probs, code, payload, k, col_probs[j].ptr, scratch, s))
                         check(lib.qgb_sample(col_probs[j].ptr, k, 1, self._next_key(), out, None, scratch, s))
-                        check(lib.qgb_collapse(state.ptr, nqubits, code, payload, k, out, 1, scratch, s))
+                        check(collapse_call(state.ptr, n_probs, code, payload, k, out, 1, scratch, s))
                         j += 1
-                check(lib.qgb_probabilities(state.ptr, nqubits, code, mq, nmeas, fin_probs.ptr, scratch, s))
-                check(lib.qgb_sample(fin_probs.ptr, nmeas, 1, self._next_key(), samples.ptr + 8 * shot, None,
-                                     scratch, s))
+                if nmeas:
+                    check(probs_call(state.ptr, n_probs, code, mq, nmeas, fin_probs.ptr, scratch, s))
+                    check(lib.qgb_sample(fin_probs.ptr, nmeas, 1, self._next_key(), samples.ptr + 8 * shot, None,
+                                         scratch, s))
+                if density:
+                    eng.axpby(mean, state, 1.0 / nshots, 1.0 if shot else 0.0)
             dec = samples.to_numpy()[:nshots]
             col = outcomes.to_numpy()[: nshots * ncol].reshape(nshots, ncol) if ncol else None
         except DeviceOutOfMemory:
@@ -297,7 +465,15 @@ class GB300Methods:
             res = getattr(g, "result", None)
             if res is not None and hasattr(res, "register_samples"):
                 res.register_samples(self.samples_to_binary(col[:, j], m))
-        binary = np.asarray(self.samples_to_binary(dec, nmeas))
+        binary = np.asarray(self.samples_to_binary(dec, nmeas)) if nmeas else None
+        if density:
+            QuantumState, CircuitResult = self._result_classes()
+            if circuit.measurements:
+                result = CircuitResult(mean, circuit.measurements, backend=self, samples=binary, nshots=nshots)
+            else:
+                result = QuantumState(mean, backend=self)
+            circuit._final_state = result
+            return result
         result = self._outcomes_class()(circuit.measurements, backend=self, samples=binary, nshots=nshots)
         if hasattr(result, "_repeated_execution_frequencies"):  # as backends/abstract.py:2631-2633
             result._repeated_execution_frequencies = collections.Counter(
@@ -311,10 +487,12 @@ class GB300Methods:
         state that agrees with outcome ``shot[0]`` of ``qubits`` (qubits[0]
         the most significant bit), divided by its norm, zeros elsewhere.  On
         the device and in place (qibojit's convention); returns the state."""
-        if density_matrix:
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
         st = self._as_device_state(state)
         outcome = int(np.asarray(shot).reshape(-1)[0])
+        if density_matrix or isinstance(st, DeviceDensity):
+            # _collapse_density_matrix (:3249-3277): rows and columns, over the kept trace
+            self.engine_gb.density_collapse(st, list(qubits), outcome, normalize)
+            return st
         self.engine_gb.collapse(st, list(qubits), outcome, normalize)
         return st
 
@@ -369,9 +547,9 @@ class GB300Methods:
 
     # -- measurement --------------------------------------------------------
     def calculate_probabilities(self, state, qubits, nqubits, density_matrix=False):
-        if density_matrix:
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
         st = self._as_device_state(state)
+        if density_matrix or isinstance(st, DeviceDensity):
+            return self.engine_gb.density_probabilities(st, list(qubits))
         return self.engine_gb.probabilities(st, list(qubits))
 
     def _device_probs(self, probabilities):
@@ -432,6 +610,11 @@ class GB300Methods:
             xs.append(x)
             zs.append(z)
             cs.append(float(np.real(coef)))
+        if isinstance(st, DeviceDensity):  # Re Tr(P rho) per term (:2985-3030)
+            val = self.engine_gb.density_expect_pauli(st, xs, zs, cs) if cs else 0.0
+            if const:
+                val += const * self.engine_gb.density_trace(st)
+            return val
         val = self.engine_gb.expect_pauli(st, xs, zs, cs) if cs else 0.0
         if const:
             val += const * self.engine_gb.norm2(st)

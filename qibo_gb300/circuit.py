@@ -18,12 +18,10 @@ class Circuit:
     def __init__(self, nqubits: int, density_matrix: bool = False, accelerators=None, **kwargs):
         if not isinstance(nqubits, int) or nqubits < 1:
             raise ValueError(f"nqubits must be a positive integer, got {nqubits}")
-        if density_matrix:
-            raise NotImplementedError("qibo_gb300 simulates state vectors only")
         if accelerators:
             raise NotImplementedError("multi-device (distributed) circuits are not supported")
         self.nqubits = nqubits
-        self.density_matrix = False
+        self.density_matrix = bool(density_matrix)
         self.accelerators = None
         self.queue = []
         self.measurements = []
@@ -59,11 +57,13 @@ class Circuit:
                 measurement.collapse = True
                 self.has_collapse = True
                 self.measurements.remove(measurement)
+        if isinstance(gate, G.UnitaryChannel):  # models/circuit.py:697-698
+            self.has_unitary_channel = True
         return None
 
     @property
     def repeated_execution(self) -> bool:
-        """models/circuit.py:321-324 (no noise channels here)."""
+        """models/circuit.py:321-324."""
         return self.has_collapse or (self.has_unitary_channel and not self.density_matrix)
 
     @property
@@ -71,7 +71,9 @@ class Circuit:
         return len(self.queue)
 
     def __add__(self, other: "Circuit") -> "Circuit":
-        c = Circuit(max(self.nqubits, other.nqubits))
+        if self.density_matrix != other.density_matrix:
+            raise ValueError("Cannot add circuits with different density_matrix settings.")
+        c = Circuit(max(self.nqubits, other.nqubits), density_matrix=self.density_matrix)
         c.add(self.queue)
         c.add(other.queue)
         return c
@@ -82,7 +84,7 @@ class Circuit:
         this circuit's alone."""
         import copy as _copy
 
-        c = Circuit(self.nqubits)
+        c = Circuit(self.nqubits, density_matrix=self.density_matrix)
         c.add([_copy.deepcopy(g) for g in self.queue] if deep else list(self.queue))
         return c
 
@@ -125,8 +127,8 @@ class Circuit:
     def fuse(self, max_qubits: int = 2) -> "Circuit":
         if not 1 <= max_qubits <= 5:
             raise ValueError("max_qubits must be between 1 and 5")
-        c = Circuit(self.nqubits)
-        c.queue = fuse_gates(self.queue, max_qubits, G.FusedGate, lambda g: isinstance(g, G.M))
+        c = Circuit(self.nqubits, density_matrix=self.density_matrix)
+        c.queue = fuse_gates(self.queue, max_qubits, G.FusedGate, lambda g: isinstance(g, (G.M, G.Channel)))
         c.measurements = list(self.measurements)
         return c
 

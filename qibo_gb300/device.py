@@ -4,7 +4,9 @@ A ``DeviceState`` owns a device buffer of ``2**nqubits`` complex amplitudes
 (complex128: 16 B, complex64: 8 B) laid out exactly like the reference's
 numpy state vector (index bit ``n-1-q`` is qubit ``q``).  It quacks like a
 1-D numpy array where qibo's result objects need it (``shape``, ``dtype``,
-``__array__``, ``tolist``), and is copied to the host only when asked.
+``__array__``, ``tolist``), and is copied to the host only when asked.  A
+``DeviceDensity`` is a density matrix stored the same way as the 2n-qubit
+vector of its row-major entries.
 """
 
 from __future__ import annotations
@@ -207,5 +209,85 @@ class DeviceState(DeviceArray):
         check(self.rt.lib.qgb_state_cast(self.ptr, self.code, out.ptr, out.code, self.nqubits, self.rt.stream))
         return out
 
+    # -- arithmetic with real scalars and same-shape states (new arrays), as
+    #    the reference's channel code combines states (gates/channels.py:702-706)
+    def __mul__(self, c):
+        if np.iscomplexobj(c) and np.imag(c) != 0:
+            return NotImplemented
+        if not np.isscalar(c) and np.ndim(c) != 0:
+            return NotImplemented
+        out = self.copy()
+        check(self.rt.lib.qgb_state_scale(out.ptr, out.nqubits, out.code, float(np.real(c)), self.rt.stream))
+        return out
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self * -1.0
+
+    def _combine(self, other, a: float):
+        if not isinstance(other, DeviceState) or other.nqubits != self.nqubits or other.shape != self.shape:
+            return NotImplemented
+        out = self.copy()
+        if other.code != out.code:
+            other = other.astype(out.dtype)
+        check(self.rt.lib.qgb_state_axpby(out.ptr, other.ptr, out.nqubits, out.code, a, 1.0, self.rt.stream))
+        return out
+
+    def __add__(self, other):
+        return self._combine(other, 1.0)
+
+    def __sub__(self, other):
+        return self._combine(other, -1.0)
+
     def __repr__(self):
         return f"DeviceState(nqubits={self.nqubits}, dtype={self.dtype.name})"
+
+
+class DeviceDensity(DeviceState):
+    """Density matrix of ``nsys`` qubits resident in device memory: the
+    (2^n, 2^n) matrix in row-major order, i.e. the 2n-qubit vector
+    v[i 2^n + j] = rho[i, j] (the reference's ``rho.ravel()``,
+    backends/abstract.py:2234-2241).  ``nqubits`` is the vector's 2n (what
+    the state-vector entry points take); ``shape`` is the matrix's, so qibo's
+    results see a density matrix (result.py:46)."""
+
+    def __init__(self, nsys: int, dtype="complex128", rt: Runtime | None = None, ptr: int | None = None):
+        self.nsys = int(nsys)
+        self.nqubits = 2 * self.nsys
+        self.code = dtype_code(dtype)
+        DeviceArray.__init__(self, (2**self.nsys, 2**self.nsys), dtype, rt, ptr)
+
+    @classmethod
+    def zero(cls, nsys: int, dtype="complex128") -> "DeviceDensity":
+        """|0...0><0...0|: the 2n-qubit basis vector 0."""
+        rho = cls(nsys, dtype)
+        check(rho.rt.lib.qgb_state_zero(rho.ptr, rho.nqubits, rho.code, rho.rt.stream))
+        return rho
+
+    @classmethod
+    def from_numpy(cls, arr, dtype=None) -> "DeviceDensity":
+        arr = np.asarray(arr)
+        d = arr.shape[0] if arr.ndim == 2 else 0
+        if arr.ndim != 2 or arr.shape[1] != d or d < 2 or d & (d - 1):
+            raise ValueError(f"a density matrix has shape (2**n, 2**n), got {arr.shape}")
+        dtype = np.dtype(dtype or (arr.dtype if arr.dtype in (np.complex64, np.complex128) else np.complex128))
+        rho = cls(d.bit_length() - 1, dtype)
+        rho.rt.h2d(rho.ptr, np.ascontiguousarray(arr, dtype=dtype))
+        return rho
+
+    def copy(self) -> "DeviceDensity":
+        out = DeviceDensity(self.nsys, self.dtype, self.rt)
+        check(self.rt.lib.qgb_memcpy_d2d(out.ptr, self.ptr, self.nbytes, self.rt.stream))
+        return out
+
+    def astype(self, dtype, copy: bool = True) -> "DeviceDensity":
+        dtype = np.dtype(dtype)
+        if dtype == self.dtype:
+            return self.copy() if copy else self
+        out = DeviceDensity(self.nsys, dtype, self.rt)
+        check(self.rt.lib.qgb_state_cast(self.ptr, self.code, out.ptr, out.code, self.nqubits, self.rt.stream))
+        return out
+
+    def __repr__(self):
+        return f"DeviceDensity(nqubits={self.nsys}, dtype={self.dtype.name})"

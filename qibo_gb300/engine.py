@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import QgbOp, check, double_array, int_array
-from .device import DeviceArray, DeviceState, Runtime
+from .device import DeviceArray, DeviceDensity, DeviceState, Runtime
 
 GateDesc = Tuple[Sequence[int], Sequence[int], np.ndarray]
 
@@ -189,16 +189,61 @@ class Engine:
         (``qubits[0]`` the most significant outcome bit); ``outcome`` is an
         int or a device int64 array whose first element is the outcome."""
         qubits = list(qubits)
-        if not isinstance(outcome, DeviceArray):
-            k = int(outcome)
-            if not 0 <= k < 2 ** len(qubits):
-                raise ValueError(f"outcome {k} outside the {2 ** len(qubits)} outcomes of {len(qubits)} qubits")
-            dev = DeviceArray((1,), np.int64, self.rt)
-            self.rt.h2d(dev.ptr, np.array([k], dtype=np.int64))
-            outcome = dev
+        outcome = self._outcome_array(outcome, len(qubits))
         scratch = self.rt.scratch(self.lib.qgb_norm_scratch_bytes())
         check(self.lib.qgb_collapse(state.ptr, state.nqubits, state.code, int_array(qubits), len(qubits),
                                     outcome.ptr, int(bool(normalize)), scratch, self.rt.stream))
+
+    def _outcome_array(self, outcome, nq: int) -> DeviceArray:
+        if isinstance(outcome, DeviceArray):
+            return outcome
+        k = int(outcome)
+        if not 0 <= k < 2**nq:
+            raise ValueError(f"outcome {k} outside the {2 ** nq} outcomes of {nq} qubits")
+        dev = DeviceArray((1,), np.int64, self.rt)
+        self.rt.h2d(dev.ptr, np.array([k], dtype=np.int64))
+        return dev
+
+    # -- density matrices --------------------------------------------------
+    def density_probabilities(self, rho: DeviceDensity, qubits: Sequence[int]) -> DeviceArray:
+        """Marginal probabilities (FP64, device) of ``qubits`` (in that
+        order) from the diagonal of ``rho``."""
+        qubits = list(qubits)
+        out = DeviceArray((2 ** len(qubits),), np.float64, self.rt)
+        scratch = self.rt.scratch(self.lib.qgb_density_scratch_bytes())
+        check(self.lib.qgb_density_probabilities(rho.ptr, rho.nsys, rho.code, int_array(qubits), len(qubits),
+                                                 out.ptr, scratch, self.rt.stream))
+        return out
+
+    def density_trace(self, rho: DeviceDensity) -> float:
+        return float(self.density_probabilities(rho, []).to_numpy()[0])
+
+    def density_collapse(self, rho: DeviceDensity, qubits: Sequence[int], outcome, normalize: bool = True):
+        """Project rows and columns of ``rho`` onto ``outcome`` of ``qubits``
+        (int or device int64 array), divided by the kept trace."""
+        qubits = list(qubits)
+        dev = self._outcome_array(outcome, len(qubits))
+        scratch = self.rt.scratch(self.lib.qgb_density_scratch_bytes())
+        check(self.lib.qgb_density_collapse(rho.ptr, rho.nsys, rho.code, int_array(qubits), len(qubits), dev.ptr,
+                                            int(bool(normalize)), scratch, self.rt.stream))
+
+    def density_expect_pauli(self, rho: DeviceDensity, xmask: Sequence[int], zmask: Sequence[int],
+                             coef: Sequence[float]) -> float:
+        """sum_t coef[t] Re Tr(P_t rho), P_t given by qubit bit masks."""
+        n = len(coef)
+        xm = (C.c_uint64 * max(1, n))(*[int(x) for x in xmask])
+        zm = (C.c_uint64 * max(1, n))(*[int(z) for z in zmask])
+        out = DeviceArray((1,), np.float64, self.rt)
+        scratch = self.rt.scratch(self.lib.qgb_density_scratch_bytes())
+        check(self.lib.qgb_density_expect_pauli(rho.ptr, rho.nsys, rho.code, xm, zm, double_array(coef), n, out.ptr,
+                                                scratch, self.rt.stream))
+        return float(out.to_numpy()[0])
+
+    def axpby(self, y: DeviceState, x: DeviceState, a: float, b: float):
+        """y = a x + b y (same size and precision)."""
+        if y.nqubits != x.nqubits or y.code != x.code:
+            raise ValueError("axpby needs arrays of the same size and precision")
+        check(self.lib.qgb_state_axpby(y.ptr, x.ptr, y.nqubits, y.code, float(a), float(b), self.rt.stream))
 
     def expect_pauli(self, state: DeviceState, xmask: Sequence[int], zmask: Sequence[int],
                      coef: Sequence[float]) -> float:

@@ -343,3 +343,9 @@ def fused_matrix(target_qubits: Sequence[int], gates, backend=None) -> np.ndarra
         spec = "".join(g_out + g_in) + "," + "".join(out_ax + in_ax) + "->" + "".join(new + in_ax)
         total = np.einsum(spec, mt, total)
     return total.reshape(2**k, 2**k)
+
+
+# noise channels (gates/channels.py), in the gates namespace as in qibo
+from .channels import (AmplitudeDampingChannel, Channel, DepolarizingChannel, KrausChannel,  # noqa: E402
+                       PauliNoiseChannel, PhaseDampingChannel, ReadoutErrorChannel, ResetChannel,
+                       ThermalRelaxationChannel, UnitaryChannel)

@@ -210,6 +210,34 @@ def main(src: str):
         constant=fs["constant"]))
     meta["fromsamples"] = fs
 
+    # 9. density matrices: gates and every channel kind, probabilities from
+    #    the diagonal, Pauli-sum energy, collapse (density_cases.py)
+    sys.path.insert(0, HERE)
+    import density_cases as dc
+
+    dm_meta = {}
+    for name, (nq, build, seed) in dc.CASES.items():
+        c = build(gates, Circuit)
+        init = None if seed is None else dc.random_rho(nq, seed)
+        res = c(initial_state=None if init is None else init.copy())
+        final = np.asarray(res.state())
+        if init is not None:
+            out[f"{name}_init"] = init
+        if name in dc.SAMPLED:
+            idx = dc.sample_indices(nq, dc.SAMPLED[name])
+            out[f"{name}_idx"] = idx
+            out[f"{name}_vals"] = final.ravel()[idx]
+        else:
+            out[f"{name}_final"] = final
+            out[f"{name}_collapse"] = backend.collapse_state(final.copy(), [1], np.array([1]), nq,
+                                                             density_matrix=True)
+        for i, qs in enumerate(dc.PROB_SETS[name]):
+            out[f"{name}_probs_{i}"] = np.asarray(res.probabilities(qs))
+        out[f"{name}_tfim"] = np.array(TFIM(nq, h=0.5, dense=False).expectation(c))
+        out[f"{name}_purity"] = np.array(np.real(np.trace(final @ final)))
+        dm_meta[name] = {"nqubits": nq, "ngates": len(c.queue)}
+    meta["density"] = dm_meta
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **out)
     with open(os.path.join(HERE, "reference_vectors.json"), "w") as f:
         json.dump(meta, f, indent=1)

@@ -211,3 +211,55 @@ class HostLib:
         h = np.array(self._view(ham, np.complex128, 4**n)).reshape(2**n, 2**n)
         self._view(out, np.float64, 1)[0] = float(np.vdot(st, h @ st).real)
         return 0
+
+    # -- density matrices (the 2n-qubit vector of rho) ---------------------------
+    def _rho(self, ptr, n, code) -> np.ndarray:
+        return self._state(ptr, 2 * n, code).reshape(2**n, 2**n)
+
+    def qgb_density_scratch_bytes(self):
+        return 0
+
+    def qgb_density_probabilities(self, ptr, n, code, qubits, nq, out, scratch, stream):
+        self.calls["qgb_density_probabilities"] += 1
+        rho = self._rho(ptr, n, code).astype(np.complex128)
+        if nq == 0:
+            p = [float(np.real(np.trace(rho)))]
+        else:
+            p = ref.calculate_probabilities_density(rho, list(qubits)[:nq], n)
+        self._view(out, np.float64, 2**nq)[:] = p
+        return 0
+
+    def qgb_density_collapse(self, ptr, n, code, qubits, nq, outcome, normalize, scratch, stream):
+        self.calls["qgb_density_collapse"] += 1
+        rho = self._rho(ptr, n, code)
+        shot = int(self._view(outcome, np.int64, 1)[0])
+        rho[:] = ref.collapse_density(rho.astype(np.complex128), list(qubits)[:nq], shot, n, bool(normalize))
+        return 0
+
+    def qgb_density_expect_pauli(self, ptr, n, code, xmask, zmask, coef, nterms, out, scratch, stream):
+        self.calls["qgb_density_expect_pauli"] += 1
+        rho = self._rho(ptr, n, code).astype(np.complex128)
+        terms, tq, cf = [], [], []
+        for t in range(nterms):
+            x, z = int(xmask[t]), int(zmask[t])
+            qs = [q for q in range(n) if ((x | z) >> q) & 1]
+            terms.append("".join("Y" if (x >> q) & (z >> q) & 1 else "X" if (x >> q) & 1 else "Z" for q in qs))
+            tq.append(tuple(qs))
+            cf.append(float(coef[t]))
+        self._view(out, np.float64, 1)[0] = ref.exp_value_observable_symbolic_density(rho, terms, tq, cf, n)
+        return 0
+
+    def qgb_state_axpby(self, y, x, n, code, a, b, stream):
+        self.calls["qgb_state_axpby"] += 1
+        yv, xv = self._state(y, n, code), self._state(x, n, code)
+        yv[:] = a * xv if b == 0 else a * xv + b * yv
+        return 0
+
+    def qgb_inner_scratch_bytes(self):
+        return 0
+
+    def qgb_inner_mixed(self, a, code_a, b, code_b, n, out, scratch, stream):
+        v = np.vdot(self._state(a, n, code_a).astype(np.complex128), self._state(b, n, code_b).astype(np.complex128))
+        self._view(out, np.float64, 2)[:] = [v.real, v.imag]
+        return 0
+

@@ -155,3 +155,63 @@ def test_oracle_expectation_from_frequencies(gold):
     fs = meta["fromsamples"]
     got = ref.exp_value_from_frequencies(fs["freq"], fs["terms_qubits"], fs["coefs"], fs["qubit_map"], fs["constant"])
     assert abs(got - float(data["fromsamples_value"])) < 1e-15
+
+
+class _Recorded:
+    """A gate or channel constructor call, recorded for the oracle."""
+
+    def __init__(self, name, args):
+        self.name, self.args, self.controls = name, args, ()
+
+    def controlled_by(self, *q):
+        self.controls = tuple(q)
+        return self
+
+
+class _RecordingGates:
+    def __getattr__(self, name):
+        return lambda *args: _Recorded(name, args)
+
+
+class _RecordingCircuit:
+    def __init__(self, nqubits, density_matrix=False):
+        self.nqubits, self.queue = nqubits, []
+
+    def add(self, op):
+        self.queue.append(op)
+
+    def ops(self):
+        return [(op.name, op.args, op.controls) for op in self.queue]
+
+
+def _density_cases():
+    import sys
+
+    sys.path.insert(0, GOLD)
+    import density_cases
+
+    return density_cases
+
+
+@pytest.mark.parametrize("name", ["dm_noisy4", "dm_noisy6", "dm_layers8"])
+def test_oracle_density_circuits(gold, name):
+    """The oracle's density-matrix restatement (gates, every channel kind,
+    diagonal probabilities, Pauli-sum energy, collapse) against the
+    reference's own outputs for the circuits of tests/golden/density_cases.py."""
+    data, meta = gold
+    dc = _density_cases()
+    n, build, seed = dc.CASES[name]
+    c = build(_RecordingGates(), _RecordingCircuit)
+    rho0 = data[f"{name}_init"] if seed is not None else None
+    rho = ref.execute_density(c.ops(), n, rho0)
+    if name in dc.SAMPLED:
+        np.testing.assert_allclose(rho.ravel()[data[f"{name}_idx"]], data[f"{name}_vals"], atol=1e-13)
+    else:
+        np.testing.assert_allclose(rho, data[f"{name}_final"], atol=1e-13)
+        np.testing.assert_allclose(ref.collapse_density(rho, [1], 1, n), data[f"{name}_collapse"], atol=1e-13)
+    for i, qs in enumerate(dc.PROB_SETS[name]):
+        np.testing.assert_allclose(ref.calculate_probabilities_density(rho, qs, n), data[f"{name}_probs_{i}"],
+                                   atol=1e-13)
+    terms, tq, cf = ref.tfim_terms(n, 0.5)
+    assert abs(ref.exp_value_observable_symbolic_density(rho, terms, tq, cf, n) - float(data[f"{name}_tfim"])) < 1e-12
+    assert abs(np.real(np.trace(rho @ rho)) - float(data[f"{name}_purity"])) < 1e-12
