@@ -81,6 +81,56 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return __longlong_as_double((long long)(sign | (e != 0 ? normal : sub)));
 }
 
+// f^2 of a float as an exact double with integer operations only: the
+// 24-bit mantissa squared is a 48-bit integer, placed under the exponent
+// 2e - 300 (subnormals as exponent 1 without the implicit bit); infinities
+// and NaNs give +inf / NaN.
+__device__ __forceinline__ double sq_exact(float f) {
+  const uint32_t u = __float_as_uint(f) & 0x7FFFFFFFu;
+  const uint32_t e = u >> 23;
+  const uint32_t m = (u & 0x7FFFFFu) | (e ? 0x800000u : 0u);
+  const uint64_t q = (uint64_t)m * m;
+  const int p = 63 - __clzll(q | 1ull);
+  const uint64_t E = (uint64_t)(p + 2 * (int)(e ? e : 1u) - 300 + 1023);
+  const uint64_t fin = q == 0 ? 0ull : (E << 52) | ((q << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  const uint64_t special = 0x7FF0000000000000ull | ((u & 0x7FFFFFu) ? (1ull << 51) : 0ull);
+  return __longlong_as_double((long long)(e == 0xFFu ? special : fin));
+}
+
+// Double-float accumulator for sums of |a|^2 off the FP64 pipe (GB300 runs
+// FP64 at about 1/64 of FP32): value hi + lo, every addition an error-free
+// two-sum into hi with the rounding error carried in lo, renormalised after
+// each step, so a partial keeps about 48 bits; partials are flushed to FP64.
+struct DFAcc {
+  float hi, lo;
+};
+
+__device__ __forceinline__ DFAcc df_add2(DFAcc s, float p, float e) {  // s + (p + e), |e| << |p|
+  const float t = s.hi + p;
+  const float bp = t - s.hi;
+  const float err = (s.hi - (t - bp)) + (p - bp);
+  const float lo = s.lo + (err + e);
+  const float h = t + lo;
+  DFAcc r;
+  r.lo = lo - (h - t);
+  r.hi = h;
+  return r;
+}
+
+// x = hi + lo (+ a remainder below 2^-47 |x|) as floats, with integer
+// operations and one integer-to-float conversion; valid for 2^-60 <= |x| <
+// 2^60 (false otherwise)
+__device__ __forceinline__ bool d_split(double x, float* hi, float* lo) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e < -60 || e >= 60) return false;
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  *hi = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+  const float r = __uint2float_rn((uint32_t)(b & 0x1FFFFFFFu));  // the 29 bits below, rounded to 24
+  *lo = __uint_as_float(__float_as_uint(r * __uint_as_float((uint32_t)(e - 52 + 127) << 23)) | sign);
+  return true;
+}
+
 struct TC64 {
   typedef float2 S;   // storage
   typedef float2 V;   // value computed on
@@ -93,12 +143,20 @@ struct TC64 {
   __device__ static V mul(V a, V b) { return cmul(a, b); }
   __device__ static V fma(V a, V b, V acc) { return cfma(a, b, acc); }
   __device__ static V row2(V u0, V a0, V u1, V a1) { return cfma(u1, a1, cmul(u0, a0)); }
-  // x^2 and y^2 of floats are exact in FP64, so one rounding in all: the
-  // FP64 pipe sees one multiply and one FMA, no conversions
-  __device__ static double abs2(V a) {
-    const double x = f2d_exact(a.x), y = f2d_exact(a.y);
-    return ::fma(x, x, y * y);
+  // x^2 and y^2 of floats are exact doubles (formed with integer
+  // operations), so one FP64 addition gives the correctly rounded |a|^2,
+  // the value of fma(x, x, y * y)
+  __device__ static double abs2(V a) { return sq_exact(a.x) + sq_exact(a.y); }
+  // sums of |a|^2: double-float partials (exact squares as float pairs),
+  // flushed to FP64 by acc_value
+  typedef DFAcc Acc;
+  __device__ static Acc acc_zero() { return DFAcc{0.f, 0.f}; }
+  __device__ static Acc acc_add(Acc s, V a, int) {
+    const float px = a.x * a.x, py = a.y * a.y;
+    s = df_add2(s, px, fmaf(a.x, a.x, -px));
+    return df_add2(s, py, fmaf(a.y, a.y, -py));
   }
+  __device__ static double acc_value(Acc s) { return f2d_exact(s.hi) + f2d_exact(s.lo); }
   // acc + |a|^2 as two FMAs (two FP64 operations instead of three)
   __device__ static double acc2(double acc, V a) {
     const double x = f2d_exact(a.x), y = f2d_exact(a.y);
@@ -131,6 +189,28 @@ struct TC128 {
   __device__ static V row2(V u0, V a0, V u1, V a1) { return cfma(u1, a1, cmul(u0, a0)); }
   __device__ static double abs2(V a) { return fma_d(a.x, a.x, a.y * a.y); }
   __device__ static double acc2(double acc, V a) { return ::fma(a.x, a.x, ::fma(a.y, a.y, acc)); }
+  // sums of |a|^2: amplitudes with ``alt`` set (every other loop step, the
+  // same for a whole warp) go to a double-float partial through d_split,
+  // the others to an FP64 partial, which halves the FP64 work; values
+  // outside d_split's range take the FP64 partial
+  struct Acc {
+    double d;
+    DFAcc f;
+  };
+  __device__ static Acc acc_zero() { return Acc{0.0, DFAcc{0.f, 0.f}}; }
+  __device__ static Acc acc_add(Acc s, V a, int alt) {
+    float xh, xl, yh, yl;
+    if (alt && d_split(a.x, &xh, &xl) && d_split(a.y, &yh, &yl)) {
+      const float px = xh * xh, py = yh * yh;
+      // x^2 = xh^2 + (2 xh + xl) xl, the first product split exactly
+      s.f = df_add2(s.f, px, fmaf(2.f * xh + xl, xl, fmaf(xh, xh, -px)));
+      s.f = df_add2(s.f, py, fmaf(2.f * yh + yl, yl, fmaf(yh, yh, -py)));
+    } else {
+      s.d = acc2(s.d, a);
+    }
+    return s;
+  }
+  __device__ static double acc_value(Acc s) { return s.d + (f2d_exact(s.f.hi) + f2d_exact(s.f.lo)); }
   __device__ static double fma_d(double a, double b, double c) { return ::fma(a, b, c); }
   __device__ static V scale(V a, double s) { return make_double2(a.x * s, a.y * s); }
   __device__ static V neg(V a) { return make_double2(-a.x, -a.y); }

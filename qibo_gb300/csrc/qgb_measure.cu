@@ -65,6 +65,7 @@ __device__ __forceinline__ i64 deposit(i64 v, const int* pos, int n) {
 
 struct ProbGeom {
   int n, nq, u;
+  u64 umask;  // unmeasured positions
   int mpos[QGB_MAXQ];  // measured bit positions, output-bit order: mpos[j] <-> output bit j
   int msorted[QGB_MAXQ];  // measured positions ascending
   int upos[QGB_MAXQ];  // unmeasured positions ascending
@@ -95,9 +96,15 @@ __global__ void __launch_bounds__(256) k_probs_thread(const typename T::S* __res
   for (i64 j = blockIdx.x * (i64)blockDim.x + threadIdx.x; j < nout; j += stride) {
     i64 base = 0;
     for (int b = 0; b < g.nq; ++b) base |= ((j >> b) & 1) << g.mpos[b];
-    double acc = 0.0;
-    for (i64 r = 0; r < nr; ++r) acc = T::acc2(acc, T::load(psi, base | deposit(r, g.upos, g.u)));
-    out[j] = acc;
+    typename T::Acc acc = T::acc_zero();
+    // unmeasured offsets in order: a counter under the mask
+    i64 off = 0;
+    const i64 step = (i64)1 << g.upos[0];
+    for (i64 r = 0; r < nr; ++r) {
+      acc = T::acc_add(acc, T::load(psi, base | off), (int)(r & 1));
+      off = (i64)(((u64)off | ~g.umask) + (u64)step) & (i64)g.umask;
+    }
+    out[j] = T::acc_value(acc);
   }
 }
 
@@ -109,15 +116,21 @@ __global__ void __launch_bounds__(256) k_probs_block(const typename T::S* __rest
   const int p = blockIdx.x % parts;
   i64 base = 0;
   for (int b = 0; b < g.nq; ++b) base |= ((j >> b) & 1) << g.mpos[b];
-  double acc = 0.0;
+  typename T::Acc acc = T::acc_zero();
   const i64 r0 = (i64)p * per_part;
-  for (i64 r = r0 + threadIdx.x; r < r0 + per_part; r += blockDim.x) {
-    // unmeasured index r -> amplitude index: insert zeros at measured positions
-    const i64 idx = insert_zeros_n(r, g.msorted, g.nq) | base;
-    acc = T::acc2(acc, T::load(psi, idx));
+  // unmeasured index r -> amplitude index: zeros inserted at the measured
+  // positions once, then a counter under the unmeasured mask advanced by
+  // the deposited stride (carries skip the measured bits)
+  i64 off = insert_zeros_n(r0 + threadIdx.x, g.msorted, g.nq);
+  const u64 step = (u64)insert_zeros_n(blockDim.x, g.msorted, g.nq);
+  int it = 0;
+#pragma unroll 4
+  for (i64 r = r0 + threadIdx.x; r < r0 + per_part; r += blockDim.x, ++it) {
+    acc = T::acc_add(acc, T::load(psi, off | base), it & 1);
+    off = (i64)(((u64)off | ~g.umask) + step) & (i64)g.umask;
   }
-  acc = block_sum256(acc);
-  if (threadIdx.x == 0) dst[blockIdx.x] = acc;
+  const double sum = block_sum256(T::acc_value(acc));
+  if (threadIdx.x == 0) dst[blockIdx.x] = sum;
 }
 
 // out[j] = sum_p src[j*parts + p], one warp per output, fixed order
@@ -161,8 +174,12 @@ int probs_impl(const void* state, int n, const int* qubits, int nq, double* out,
     mbits.push_back(n - 1 - q);
   }
   int ui = 0;
+  g.umask = 0;
   for (int b = 0; b < n; ++b)
-    if (std::find(mbits.begin(), mbits.end(), b) == mbits.end()) g.upos[ui++] = b;
+    if (std::find(mbits.begin(), mbits.end(), b) == mbits.end()) {
+      g.upos[ui++] = b;
+      g.umask |= 1ull << b;
+    }
   std::vector<int> sorted = mbits;
   std::sort(sorted.begin(), sorted.end());
   for (int j = 0; j < nq; ++j) g.msorted[j] = sorted[j];
@@ -234,11 +251,13 @@ int qgb_probabilities(const void* state, int nqubits, int dtype, const int* qubi
 template <typename T>
 __global__ void __launch_bounds__(256) k_norm_part(const typename T::S* __restrict__ psi, i64 N,
                                                    double* __restrict__ part) {
-  double acc = 0.0;
+  typename T::Acc acc = T::acc_zero();
   const i64 stride = (i64)gridDim.x * blockDim.x;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) acc = T::acc2(acc, T::load(psi, i));
-  acc = block_sum256(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  int it = 0;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride, ++it)
+    acc = T::acc_add(acc, T::load(psi, i), it & 1);
+  const double sum = block_sum256(T::acc_value(acc));
+  if (threadIdx.x == 0) part[blockIdx.x] = sum;
 }
 
 __global__ void k_final_sum(const double* __restrict__ part, int nparts, double* __restrict__ out) {
@@ -383,17 +402,18 @@ __global__ void __launch_bounds__(256) k_draw(const double* __restrict__ probs, 
 
 // Sampling every qubit straight from the state (no 2^n probability vector):
 // chunk sums of |psi|^2 over 64 amplitudes, then an in-chunk recompute.  The
-// in-chunk running sum adds the same FP64 terms in the same order as the
-// chunk sum, so both CDF levels agree.
+// in-chunk running sum accumulates the same terms in the same order, with
+// the same partial (FP64 or double-float by position parity), as the chunk
+// sum, so both CDF levels agree.
 template <typename T>
 __global__ void __launch_bounds__(256) k_state_chunk_sums(const typename T::S* __restrict__ psi, i64 N, i64 nchunks,
                                                           double* __restrict__ chunk) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 c = blockIdx.x * (i64)blockDim.x + threadIdx.x; c < nchunks; c += stride) {
-    double acc = 0.0;
-    const i64 e = imin64(N, (c + 1) * QGB_CHUNK);
-    for (i64 i = c * QGB_CHUNK; i < e; ++i) acc = T::acc2(acc, T::load(psi, i));
-    chunk[c] = acc;
+    typename T::Acc acc = T::acc_zero();
+    const i64 b = c * QGB_CHUNK, e = imin64(N, b + QGB_CHUNK);
+    for (i64 i = b; i < e; ++i) acc = T::acc_add(acc, T::load(psi, i), (int)((i - b) & 1));
+    chunk[c] = T::acc_value(acc);
   }
 }
 
@@ -411,15 +431,16 @@ __global__ void __launch_bounds__(256) k_draw_state(const typename T::S* __restr
       const i64 mid = (lo + hi) >> 1;
       if (cdf[mid] > target) hi = mid; else lo = mid + 1;
     }
-    double run = lo > 0 ? cdf[lo - 1] : 0.0;
+    const double before = lo > 0 ? cdf[lo - 1] : 0.0;
+    typename T::Acc run = T::acc_zero();
     const i64 b = lo * QGB_CHUNK, e = imin64(N, b + QGB_CHUNK);
     i64 pick = -1, last_nz = -1;
     for (i64 i = b; i < e; ++i) {
       const typename T::V v = T::load(psi, i);
-      if (T::abs2(v) > 0.0) {
+      run = T::acc_add(run, v, (int)((i - b) & 1));  // the chunk sums' operation
+      if (T::re(v) != 0.0 || T::im(v) != 0.0) {
         last_nz = i;
-        run = T::acc2(run, v);  // the chunk sums' operation (zeros add exactly nothing there)
-        if (run > target) { pick = i; break; }
+        if (before + T::acc_value(run) > target) { pick = i; break; }
       }
     }
     if (pick < 0) pick = last_nz;

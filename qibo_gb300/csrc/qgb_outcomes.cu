@@ -92,18 +92,19 @@ __global__ void __launch_bounds__(256) k_collapse_norm(const typename T::S* __re
                                                        double* __restrict__ part) {
   uint64_t mask, value;
   collapse_target(a, *outcome, &mask, &value);
-  double acc = 0.0;
+  typename T::Acc acc = T::acc_zero();
   const i64 stride = (i64)gridDim.x * blockDim.x;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nkept; t += stride) {
+  int it = 0;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nkept; t += stride, ++it) {
     i64 idx = t;
     for (int j = 0; j < a.nq; ++j) {
       const int p = a.sorted[j];
       idx = ((idx >> p) << (p + 1)) | (idx & ((((i64)1) << p) - 1));
     }
-    acc = T::acc2(acc, T::load(psi, idx | (i64)value));
+    acc = T::acc_add(acc, T::load(psi, idx | (i64)value), it & 1);
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  const double sum = block_sum(T::acc_value(acc));
+  if (threadIdx.x == 0) part[blockIdx.x] = sum;
 }
 
 __global__ void k_collapse_final(const double* __restrict__ part, int nparts, double* __restrict__ out) {

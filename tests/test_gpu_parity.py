@@ -269,6 +269,43 @@ def test_norm_is_fp64(backend):
     assert abs(backend.engine_gb.norm2(st) - 1.0) < 1e-13
 
 
+def _wide_range_state(n, seed, dtype):
+    """Amplitudes log-uniform over 1e-30..1 (floats: some subnormal), random
+    signs, about 1/8 exact zeros: exercises every range branch of the
+    reductions."""
+    rng = np.random.default_rng(seed)
+    mag = 10.0 ** rng.uniform(-30, 0, (2, 2**n))
+    if dtype == np.complex64:
+        mag[:, : 2**n // 64] *= 1e-12  # below the smallest normal float for some
+    sgn = rng.choice([-1.0, 1.0], (2, 2**n))
+    v = (sgn * mag)[0] + 1j * (sgn * mag)[1]
+    v[rng.random(2**n) < 0.125] = 0
+    return v.astype(dtype)
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_reductions_fp64_accuracy(backend, dtype):
+    """Norm and marginal probabilities (all qubits, a few qubits, one qubit)
+    against sums in extended precision of the same stored values: relative
+    error below 1e-13 (the complex64 partials are double-float, the complex128
+    ones half FP64, half double-float)."""
+    from qibo_gb300.device import DeviceState
+
+    n = 22
+    psi = _wide_range_state(n, 7, dtype)
+    p_exact = (psi.real.astype(np.longdouble) ** 2 + psi.imag.astype(np.longdouble) ** 2)
+    st = DeviceState.from_numpy(psi)
+    nrm = backend.engine_gb.norm2(st)
+    want = float(np.sum(p_exact))
+    assert abs(nrm - want) <= 1e-13 * want
+    for qs in ([0, 1, 2], [21], [5, 17, 0, 11, 3, 20, 8, 14, 2, 19], list(range(n))):
+        got = np.asarray(backend.calculate_probabilities(st, qs, n))
+        w = ref.order_probabilities(np.sum(p_exact.reshape((2,) * n),
+                                           axis=tuple(q for q in range(n) if q not in qs)), qs, n).ravel()
+        w = np.asarray(w, dtype=np.float64)
+        assert np.all(np.abs(got - w) <= 1e-13 * np.maximum(w, 1e-300)), qs
+
+
 def test_philox_known_answers():
     """Random123 known-answer vectors for philox4x32-10."""
     from qibo_gb300 import _lib
