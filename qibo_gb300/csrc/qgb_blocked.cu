@@ -24,17 +24,76 @@
 
 #define QGB_PASS_MAX_OPS 96
 #define QGB_PASS_MAX_COEF 1536
+#define QGB_PASS_MAX_RUNS 8
+#define QGB_PASS_MAX_RUNOPS 256
 
 int qgb_launch_gateop(void* state, int n, int dtype, const GateOp& g, cudaStream_t s);  // qgb_gates.cu
+
+// Merged phase runs.  Consecutive phase gates of a pass (each multiplies
+// the amplitudes whose index has all bits of its mask set) whose masks
+// share a part P and have at most one bit c_o outside it act together as
+// [P in j] * prod_o (c_o in j ? phi_o : 1).  With the tile index
+// j = t + 2^tb r (t the thread, r the thread's step) and the tile's
+// non-local bits, the product splits into FT[t] (ops whose c_o is a bit of
+// t), FR[r] (a bit of r) and FG (a non-local bit, or no c_o): FT and FR are
+// tabulated once per CTA, FG once per tile, so a run costs two complex
+// multiplications per amplitude instead of one per gate.  QFT layers (the
+// controlled phases after each Hadamard share its target) are such runs.
+struct PRunOp {
+  int16_t coef;  // offset of phi_o in PassParams::coef
+  uint8_t dom;   // 0: bit of t, 1: bit of r, 2: non-local bit, 3: none
+  uint8_t bit;   // position in t or r, or the global position
+};
+struct PRun {
+  int16_t first, count;  // into PassParams::rops
+};
 
 template <typename T>
 struct PassParams {
   int nops, L, m, n;
+  int nruns, tb;         // merged phase runs; thread-index bits of the tile index
   int nonloc[QGB_MAXQ];  // ascending global positions of the non-local bits
   int hiloc[QGB_MAXQ];   // ascending global positions of local bits >= m
   POp ops[QGB_PASS_MAX_OPS];
+  PRun runs[QGB_PASS_MAX_RUNS];
+  PRunOp rops[QGB_PASS_MAX_RUNOPS];
   typename T::V coef[QGB_PASS_MAX_COEF];
 };
+
+// product of the run's phases whose c_o is in domain ``dom`` with its bit set in ``bits``
+// (dom 2 also takes the ops without c_o)
+template <typename T>
+__device__ __forceinline__ typename T::V run_product(const PassParams<T>& P, const PRun& R, int dom, u64 bits) {
+  typename T::V acc = T::one();
+  for (int i = R.first; i < R.first + R.count; ++i) {
+    const PRunOp& o = P.rops[i];
+    const bool take = o.dom == dom ? ((bits >> o.bit) & 1) != 0 : (dom == 2 && o.dom == 3);
+    if (take) acc = T::mul(acc, P.coef[o.coef]);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ float2 shfl_down_v(float2 v, int o) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ double2 shfl_down_v(double2 v, int o) {
+  return make_double2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ cdf shfl_down_v(cdf v, int o) {
+  cdf r;
+  r.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, o);
+  r.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, o);
+  r.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, o);
+  r.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, o);
+  return r;
+}
+
+// shared-memory bytes of the run tables: FT, FR and FG per run
+template <typename T>
+__host__ __device__ __forceinline__ size_t run_table_bytes(int nruns, int L, int tb) {
+  return (size_t)nruns * (((size_t)1 << tb) + ((size_t)1 << (L - tb)) + 1) * sizeof(typename T::V);
+}
+__host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // One pass over the state (see the file comment); P may live in kernel
 // parameter space (k_pass) or in device memory (k_pass_dev, used by captured
@@ -54,20 +113,47 @@ __device__ __forceinline__ void pass_body(typename T::G* __restrict__ psi, i64 n
     for (int b = 0; b < L - m; ++b) o |= (i64)((h >> b) & 1) << P.hiloc[b];
     dep[h] = o;
   }
+  // run tables (see PRunOp): FT and FR once per CTA
+  const int nT = 1 << P.tb, nR = 1 << (L - P.tb);
+  V* FT = (V*)(smem_raw + align16((size_t)TN * sizeof(S) + ((size_t)nhi << 3)));
+  V* FR = FT + P.nruns * nT;
+  V* FG = FR + P.nruns * nR;
+  for (int i = threadIdx.x; i < P.nruns * nT; i += blockDim.x) FT[i] = run_product(P, P.runs[i / nT], 0, i % nT);
+  for (int i = threadIdx.x; i < P.nruns * nR; i += blockDim.x) FR[i] = run_product(P, P.runs[i / nR], 1, i % nR);
   __syncthreads();
   const int nl = P.n - L;
   const int lowmask = (1 << m) - 1;
+  const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
     i64 base = 0;
     for (int b = 0; b < nl; ++b) base |= ((t >> b) & 1) << P.nonloc[b];
     for (int j = threadIdx.x; j < TN; j += blockDim.x)
       T::store(tile, j, T::from_global(psi[base | dep[j >> m] | (j & lowmask)]));
+    // FG of every run for this tile: one warp per run, lanes over its ops
+    for (int r = threadIdx.x >> 5; r < P.nruns; r += nwarps) {
+      const PRun& R = P.runs[r];
+      V acc = T::one();
+      for (int i = R.first + lane; i < R.first + R.count; i += 32) {
+        const PRunOp& o = P.rops[i];
+        if (o.dom == 3 || (o.dom == 2 && ((base >> o.bit) & 1))) acc = T::mul(acc, P.coef[o.coef]);
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc = T::mul(acc, shfl_down_v(acc, off));
+      if (lane == 0) FG[r] = acc;
+    }
     __syncthreads();
     for (int o = 0; o < P.nops; ++o) {
       const POp& op = P.ops[o];
       if ((base & (i64)op.gmask) != (i64)op.gmask) continue;  // uniform over the CTA
-      const V* M = P.coef + op.coef;
-      apply_tile_op<T, MAXK>(tile, L, op, M);
+      if (op.kind == GK_PRUN) {
+        const int r = op.coef;
+        const V a = T::mul(FT[r * nT + (threadIdx.x & (nT - 1))], FG[r]);
+        const V* fr = FR + r * nR;
+        for (int j = threadIdx.x; j < TN; j += blockDim.x)
+          if ((j & op.lmask) == op.lmask) T::store(tile, j, T::mul(T::load(tile, j), T::mul(a, fr[j >> P.tb])));
+      } else {
+        apply_tile_op<T, MAXK>(tile, L, op, P.coef + op.coef);
+      }
       __syncthreads();
     }
     for (int j = threadIdx.x; j < TN; j += blockDim.x)
@@ -156,7 +242,6 @@ std::vector<Pass> plan_passes(const std::vector<GateOp>& ops, int n, int L, int 
 
 template <typename T>
 void pack_params(PassParams<T>* P, int n, int L, int m, const Pass& pass, const std::vector<GateOp>& ops) {
-  P->nops = (int)pass.ops.size();
   P->L = L;
   P->m = m;
   P->n = n;
@@ -166,11 +251,73 @@ void pack_params(PassParams<T>* P, int n, int L, int m, const Pass& pass, const 
   int nl = 0;
   for (int b = 0; b < n; ++b)
     if (pos_of[b] < 0) P->nonloc[nl++] = b;
+  P->tb = std::min(L, 8);  // the pass kernels run min(256, 2^L) threads (at least 32)
+  P->nruns = 0;
+  // coefficients of every op, in pass order
+  const int nops = (int)pass.ops.size();
+  std::vector<int> coef_at(nops);
   int coef = 0;
-  for (int o = 0; o < P->nops; ++o) {
-    const GateOp& g = ops[pass.ops[o]];
-    POp& po = P->ops[o];
+  for (int o = 0; o < nops; ++o) {
+    coef_at[o] = coef;
+    for (const zd& c : ops[pass.ops[o]].coef) P->coef[coef++] = T::coef(c.real(), c.imag());
+  }
+  auto mask_of = [&](int o) {
+    u64 mk = 0;
+    for (int b : ops[pass.ops[o]].cbits) mk |= 1ull << b;
+    return mk;
+  };
+  auto is_phase = [&](int o) { return ops[pass.ops[o]].kind == GK_PHASE; };
+  int npo = 0, nrops = 0;
+  int o = 0;
+  while (o < nops) {
+    // the longest run of phase gates from o whose masks have at most one bit
+    // outside their common part
+    int e = o;
+    u64 common = 0;
+    if (is_phase(o) && P->nruns < QGB_PASS_MAX_RUNS) {
+      common = mask_of(o);
+      e = o + 1;
+      while (e < nops && is_phase(e) && nrops + (e + 1 - o) <= QGB_PASS_MAX_RUNOPS) {
+        const u64 c2 = common & mask_of(e);
+        bool ok = true;
+        for (int k = o; k <= e && ok; ++k) ok = __builtin_popcountll(mask_of(k) & ~c2) <= 1;
+        if (!ok) break;
+        common = c2;
+        ++e;
+      }
+    }
+    POp& po = P->ops[npo++];
     po = POp();
+    if (e - o >= 2) {
+      const int r = P->nruns++;
+      P->runs[r].first = (int16_t)nrops;
+      P->runs[r].count = (int16_t)(e - o);
+      for (int k = o; k < e; ++k) {
+        PRunOp& ro = P->rops[nrops++];
+        ro.coef = (int16_t)coef_at[k];
+        const u64 c = mask_of(k) & ~common;
+        if (!c) {
+          ro.dom = 3;
+          ro.bit = 0;
+        } else {
+          const int b = __builtin_ctzll(c);
+          const int lp = pos_of[b];
+          if (lp < 0) { ro.dom = 2; ro.bit = (uint8_t)b; }
+          else if (lp < P->tb) { ro.dom = 0; ro.bit = (uint8_t)lp; }
+          else { ro.dom = 1; ro.bit = (uint8_t)(lp - P->tb); }
+        }
+      }
+      po.kind = GK_PRUN;
+      for (int b = 0; b < n; ++b)
+        if ((common >> b) & 1) {
+          if (pos_of[b] >= 0) po.lmask |= 1u << pos_of[b];
+          else po.gmask |= 1ull << b;
+        }
+      po.coef = r;
+      o = e;
+      continue;
+    }
+    const GateOp& g = ops[pass.ops[o]];
     po.kind = (uint8_t)g.kind;
     po.k = (uint8_t)g.tbits.size();
     for (size_t i = 0; i < g.tbits.size(); ++i) po.tpos[i] = (uint8_t)pos_of[g.tbits[i]];
@@ -178,9 +325,10 @@ void pack_params(PassParams<T>* P, int n, int L, int m, const Pass& pass, const 
       if (pos_of[b] >= 0) po.lmask |= 1u << pos_of[b];
       else po.gmask |= 1ull << b;
     }
-    po.coef = coef;
-    for (const zd& c : g.coef) P->coef[coef++] = T::coef(c.real(), c.imag());
+    po.coef = coef_at[o];
+    ++o;
   }
+  P->nops = npo;
 }
 
 template <typename T>
@@ -192,10 +340,11 @@ struct PassLaunch {
 };
 
 template <typename T>
-PassLaunch<T> pass_launch(int n, int L, int m) {
+PassLaunch<T> pass_launch(int n, int L, int m, int nruns) {
   PassLaunch<T> pl;
   pl.ntiles = (i64)1 << (n - L);
-  pl.smem = ((size_t)sizeof(typename T::S) << L) + (sizeof(i64) << (L - m));
+  pl.smem = align16(((size_t)sizeof(typename T::S) << L) + (sizeof(i64) << (L - m))) +
+            run_table_bytes<T>(nruns, L, std::min(L, 8));
   pl.status = qgb_func_smem((const void*)k_pass<T, 2>, 200 * 1024);
   if (!pl.status) pl.status = qgb_func_smem((const void*)k_pass<T, 5>, 200 * 1024);
   if (!pl.status) pl.status = qgb_func_smem((const void*)k_pass_dev<T, 2>, 200 * 1024);
@@ -218,7 +367,7 @@ template <typename T>
 int run_pass(void* state, int n, int L, int m, const Pass& pass, const std::vector<GateOp>& ops, cudaStream_t s) {
   PassParams<T>* P = new PassParams<T>();
   pack_params<T>(P, n, L, m, pass, ops);
-  const PassLaunch<T> pl = pass_launch<T>(n, L, m);
+  const PassLaunch<T> pl = pass_launch<T>(n, L, m, P->nruns);
   if (pl.status) {
     delete P;
     return pl.status;
@@ -363,7 +512,10 @@ void program_pack(Program* p) {
 
 template <typename T>
 int program_launches(Program* p, cudaStream_t s) {
-  const PassLaunch<T> pl = pass_launch<T>(p->n, p->L, p->m);
+  int nruns = 0;  // tables sized for the pass with the most runs
+  for (size_t i = 0; i < p->passes.size(); ++i)
+    nruns = std::max(nruns, ((const PassParams<T>*)(p->hparams + i * p->pbytes))->nruns);
+  const PassLaunch<T> pl = pass_launch<T>(p->n, p->L, p->m, nruns);
   if (pl.status) return pl.status;
   for (size_t i = 0; i < p->passes.size(); ++i) {
     const PassParams<T>* P = (const PassParams<T>*)((unsigned char*)p->dparams + i * p->pbytes);

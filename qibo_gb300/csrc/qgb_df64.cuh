@@ -29,8 +29,6 @@ __host__ __device__ __forceinline__ df df_split(double x) {
   return {hi, (float)(x - (double)hi)};
 }
 
-__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
-
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
@@ -174,19 +172,22 @@ struct TC128F {
   typedef cdf S;
   typedef cdf V;
   static constexpr int kind = QGB_C128;
+  __device__ static V one() { return cdf{{1.f, 0.f}, {0.f, 0.f}}; }
   static V coef(double re, double im) {
     cdf c;
     c.re = df_split(re);
     c.im = df_split(im);
     return c;
   }
+  // tiles convert with integer operations (df_split_int) and one FP64
+  // addition per double on the way back (df_join)
   __device__ static V from_global(double2 v) {
     cdf c;
-    c.re = df_split(v.x);
-    c.im = df_split(v.y);
+    c.re = df_split_int(v.x);
+    c.im = df_split_int(v.y);
     return c;
   }
-  __device__ static double2 to_global(V v) { return make_double2(df_to_double(v.re), df_to_double(v.im)); }
+  __device__ static double2 to_global(V v) { return make_double2(df_join(v.re), df_join(v.im)); }
   __device__ static V load(const S* p, int i) { return p[i]; }
   __device__ static void store(S* p, int i, V v) { p[i] = v; }
   __device__ static V mul(V a, V b) { return cdf_mul(a, b); }

@@ -15,6 +15,7 @@ struct PlainPass {
   typedef G_ S;
   typedef G_ V;
   static V coef(double re, double im) { return C::coef(re, im); }
+  __device__ static V one() { return C::coef(1.0, 0.0); }
   __device__ static V from_global(G v) { return v; }
   __device__ static G to_global(V v) { return v; }
   __device__ static V load(const S* p, int i) { return p[i]; }
@@ -30,6 +31,10 @@ struct PlainPass {
 };
 typedef PlainPass<TC64, float2> P64;
 typedef PlainPass<TC128, double2> P128;
+
+// A run of phase gates merged by the pass planner (qgb_blocked.cu): device
+// only, never produced by qgb_classify.
+#define GK_PRUN 5
 
 struct POp {
   uint8_t kind, k;
