@@ -320,6 +320,11 @@ void pack_params(PassParams<T>* P, int n, int L, int m, const Pass& pass, const 
     const GateOp& g = ops[pass.ops[o]];
     po.kind = (uint8_t)g.kind;
     po.k = (uint8_t)g.tbits.size();
+    if (g.kind == GK_DENSE && po.k <= 2) {
+      bool real = true;
+      for (const zd& c : g.coef) real = real && c.imag() == 0.0;
+      if (real) po.kind = GK_REAL;
+    }
     for (size_t i = 0; i < g.tbits.size(); ++i) po.tpos[i] = (uint8_t)pos_of[g.tbits[i]];
     for (int b : g.cbits) {
       if (pos_of[b] >= 0) po.lmask |= 1u << pos_of[b];

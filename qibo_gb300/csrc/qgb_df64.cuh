@@ -193,4 +193,20 @@ struct TC128F {
   __device__ static V mul(V a, V b) { return cdf_mul(a, b); }
   template <int D>
   __device__ static V row(const V* u, const V* a) { return cdf_row<D>(u, a); }
+  template <int D>  // u real: one error-free dot product of D terms per part
+  __device__ static V row_real(const V* u, const V* a) {
+    df x[D], yr[D], yi[D];
+    float sg[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      x[c] = u[c].re;
+      yr[c] = a[c].re;
+      yi[c] = a[c].im;
+      sg[c] = 1.f;
+    }
+    cdf r;
+    r.re = df_dot<D>(x, yr, sg);
+    r.im = df_dot<D>(x, yi, sg);
+    return r;
+  }
 };

@@ -39,13 +39,15 @@
 // level 6 is its own instruction so that it starts the accumulation), 25
 // per half and tile.
 //
-// A CTA (544 threads, one per SM: 224 KB of shared memory, 448 TMEM
+// A CTA (576 threads, one per SM: 224 KB of shared memory, 448 TMEM
 // columns) owns 4096-amplitude tiles with the index geometry of qgb_tc.cu,
-// in three roles that run as a pipeline:
-//  * warps 0-7 convert (thread t moves amplitudes t + 256 r, r < 16).  The
-//    raw tile is copied into shared memory by the bulk-copy engine one tile
-//    ahead (32 runs of 128 contiguous amplitudes), so the loads stay in
-//    flight without holding registers.  A thread reads its amplitudes,
+// in four roles that run as a pipeline:
+//  * warp 17 copies the raw tiles into shared memory with the bulk-copy
+//    engine, one tile ahead (32 runs of 128 contiguous amplitudes, a run per
+//    lane), so the loads stay in flight without holding registers and the
+//    converters never stop to issue them;
+//  * warps 0-7 convert (thread t moves amplitudes t + 256 r, r < 16).  A
+//    thread reads its amplitudes,
 //    forms their digit words, frees the raw buffer for the next copy, and
 //    writes digit slice s of A as soon as the previous tile's MMAs on slice
 //    s are done;
@@ -63,7 +65,7 @@
 // and one FP32 subtraction makes it an exact float.  The level combination
 // is an integer multiply-add chain.  Every wait on an mbarrier is bounded
 // and also ends when another role has recorded an abort; the MMA thread
-// then waits once more (bounded) for its in-flight MMAs, the converters for
+// then waits once more (bounded) for its in-flight MMAs, the copy warp for
 // an in-flight copy, and tensor memory is freed.
 //
 // Runs of unitary blocks (qgb_run_oz_chain) keep the state in a 64-bit
@@ -82,7 +84,8 @@
 #define OZ_CONV_WARPS 8                        // converter warps 0-7
 #define OZ_EPI_WARPS 8                         // epilogue warps 8-15 (lane quarter = warp mod 4)
 #define OZ_MMA_WARP (OZ_CONV_WARPS + OZ_EPI_WARPS)  // warp 16: MMA issue
-#define OZ_THREADS ((OZ_MMA_WARP + 1) * 32)    // 544
+#define OZ_COPY_WARP (OZ_MMA_WARP + 1)         // warp 17: bulk copies of the raw tiles
+#define OZ_THREADS ((OZ_COPY_WARP + 1) * 32)   // 576
 #define OZ_GROUP (OZ_CONV_WARPS * 32)          // converter threads
 #define OZ_EPI (OZ_EPI_WARPS * 32)             // epilogue threads
 #define OZ_STEPS 16     // amplitudes per converter thread per tile
@@ -503,6 +506,7 @@ __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const O
 // completion of a phase needs the waiter's previous phase to have been
 // consumed upstream):
 //   m_raw    bulk copies -> converters    the raw tile is in shared memory
+//   m_rawfree  converter -> copy warp     the raw tile has been read
 //   m_ready[s]  converter -> MMA          A slice s of tile i written
 //   m_free[s]   tcgen05.commit -> converter   the MMAs of tile i that read
 //            slice s are done (the last ones, of half 1)
@@ -510,13 +514,13 @@ __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const O
 //   m_full[h]  tcgen05.commit -> epilogue   MMAs of half h of tile i done
 //   m_tfree[h] epilogue (256 arrivals) -> MMA   half h of tile i read
 template <bool FIX>
-__global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registers
+__global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registers
     k_fused5_oz(double2* __restrict__ psi, i64 ntiles, const __grid_constant__ OzGeom geo,
                 const __grid_constant__ OzGate G, int* __restrict__ err, const uint32_t* __restrict__ fix_in,
                 uint32_t* __restrict__ fix_out, uint32_t* __restrict__ fix_zero) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t m_raw, m_ready[OZ_NSLICE], m_free[OZ_NSLICE], m_scale[2], m_full[2], m_tfree[2],
-      m_drain;
+  __shared__ __align__(8) uint64_t m_raw, m_rawfree, m_ready[OZ_NSLICE], m_free[OZ_NSLICE], m_scale[2], m_full[2],
+      m_tfree[2], m_drain;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;  // set by any role on a failed wait
   __shared__ int c_stop[2];   // the converters' decisions, written by their thread 0 before their barriers
@@ -544,6 +548,7 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
   if (tid == 0) {
     abort_flag = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_raw)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_rawfree)));
     for (int k = 0; k < OZ_NSLICE; ++k) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_ready[k])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_free[k])));
@@ -582,8 +587,8 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
   if (warp < OZ_CONV_WARPS) {
     // ---------------------------------------------------------- converters
     // The raw tile arrives in shared memory by bulk copies issued one tile
-    // ahead (warp 0, one 2 KB run per lane), so the loads of the next tile
-    // are in flight while this one converts, with no registers held.  A
+    // ahead (the copy warp, one 2 KB run per lane), so the loads of the next
+    // tile are in flight while this one converts, with no registers held.  A
     // thread reads its 16 amplitudes, turns them into their digit words Z
     // (oz_zdigits) in registers and frees the raw tile for the next copy;
     // then it writes digit slice s as soon as the previous tile's MMAs that
@@ -591,23 +596,7 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
     const int g = tid;  // 0..255
     const uint32_t aoff = geo.aoff_lo[g];
     const uint32_t mraw = smem_u32(&m_raw);
-    const uint32_t raw = s_base + OZ_OFF_RAW;
-    // run lane of warp 0: 2 r + hi, r = lane >> 1
-    const i64 run_off = ((lane & 1) ? geo.g7 : 0) + geo.ghi[lane >> 1];
-    auto issue_copy = [&](i64 tt) {  // warp 0, all lanes
-      const i64 tb = tile_base(tt, lane, my_rest);
-      if (lane == 0)
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mraw), "r"((uint32_t)OZ_RAW_BYTES)
-                     : "memory");
-      __syncwarp();
-      oz_copy_run(raw + lane * OZ_RUN, psi + tb + run_off, mraw);
-    };
     i64 t = blockIdx.x;
-    int copies = 0, consumed = 0;  // raw-tile copies issued (by warp 0) and tiles whose copy was waited for
-    if (warp == 0 && t < ntiles) {
-      issue_copy(t);
-      copies = 1;
-    }
     for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
       // this tile's raw values -> registers
       const bool got = oz_wait(mraw, (uint32_t)it & 1, abort_v);
@@ -635,10 +624,7 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       oz_bar(1);
       if (c_stop[0]) break;
-      if (warp == 0 && t + gridDim.x < ntiles) {
-        issue_copy(t + gridDim.x);
-        copies = it + 2;
-      }
+      if (g == 0) oz_arrive(smem_u32(&m_rawfree));  // raw tile read: the next copy may land
       if (FIX) {
         const int64_t bias = oz_fix_bias(fix_sh);
 #pragma unroll
@@ -681,11 +667,28 @@ __global__ void __maxnreg__(96)  // 17 warps: five share one SMSP's 16 K registe
       if (g == 0) c_stop[1] = *abort_v;
       oz_bar(1);
       if (c_stop[1]) break;
-      consumed = it + 1;
     }
-    // on an abort, a copy may still be writing the raw tile: wait for it
-    // (bounded) before the CTA's shared memory is released
-    if (g == 0 && copies > consumed) mbar_wait(mraw, (uint32_t)(copies - 1) & 1);
+  } else if (warp == OZ_COPY_WARP) {
+    // ------------------------------------------------------------- copies
+    // tile it's 32 runs of 128 amplitudes, one bulk copy per lane (run
+    // 2 r + hi for lane 2 r + hi), once the converters have read tile it - 1
+    const uint32_t mraw = smem_u32(&m_raw), mrawfree = smem_u32(&m_rawfree);
+    const uint32_t raw = s_base + OZ_OFF_RAW;
+    const i64 run_off = ((lane & 1) ? geo.g7 : 0) + geo.ghi[lane >> 1];
+    int copies = 0;
+    for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      if (copies > 0 && !__all_sync(0xffffffffu, oz_wait(mrawfree, (uint32_t)(copies - 1) & 1, abort_v))) break;
+      const i64 tb = tile_base(t, lane, my_rest);
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mraw), "r"((uint32_t)OZ_RAW_BYTES)
+                     : "memory");
+      __syncwarp();
+      oz_copy_run(raw + lane * OZ_RUN, psi + tb + run_off, mraw);
+      ++copies;
+    }
+    // after an abort the last copy may still be writing the raw tile: wait
+    // for it (bounded) before the CTA's shared memory is released
+    if (lane == 0 && copies > 0) mbar_wait(mraw, (uint32_t)(copies - 1) & 1);
   } else if (warp < OZ_MMA_WARP) {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3;                     // TMEM lane quarter (warp mod 4)

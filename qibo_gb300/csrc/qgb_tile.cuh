@@ -28,13 +28,28 @@ struct PlainPass {
     for (int c = 1; c < D; ++c) acc = cfma(u[c], a[c], acc);
     return acc;
   }
+  template <int D>  // u real (imaginary parts zero)
+  __device__ static V row_real(const V* u, const V* a) {
+    V acc;
+    acc.x = u[0].x * a[0].x;
+    acc.y = u[0].x * a[0].y;
+#pragma unroll
+    for (int c = 1; c < D; ++c) {
+      acc.x = fma(u[c].x, a[c].x, acc.x);
+      acc.y = fma(u[c].x, a[c].y, acc.y);
+    }
+    return acc;
+  }
 };
 typedef PlainPass<TC64, float2> P64;
 typedef PlainPass<TC128, double2> P128;
 
-// A run of phase gates merged by the pass planner (qgb_blocked.cu): device
-// only, never produced by qgb_classify.
+// Device-only kinds set by the pass planner (qgb_blocked.cu), never by
+// qgb_classify: a run of phase gates merged into one sweep, and a dense 1-
+// or 2-qubit gate whose matrix is real (Hadamard, RY, ...), which needs half
+// the multiplications of a complex one.
 #define GK_PRUN 5
+#define GK_REAL 6
 
 struct POp {
   uint8_t kind, k;
@@ -49,7 +64,7 @@ struct POp {
 
 __device__ __forceinline__ int ins0(int j, int p) { return ((j >> p) << (p + 1)) | (j & ((1 << p) - 1)); }
 
-template <typename T, int K>
+template <typename T, int K, bool REAL = false>
 __device__ __forceinline__ void apply_dense_tile(typename T::S* tile, int L, const POp& op,
                                                  const typename T::V* __restrict__ M) {
   constexpr int D = 1 << K;
@@ -80,7 +95,10 @@ __device__ __forceinline__ void apply_dense_tile(typename T::S* tile, int L, con
 #pragma unroll
     for (int mm = 0; mm < D; ++mm) v[mm] = T::load(tile, j0 + off[mm]);
 #pragma unroll
-    for (int r = 0; r < D; ++r) T::store(tile, j0 + off[r], T::template row<D>(M + r * D, v));
+    for (int r = 0; r < D; ++r) {
+      if constexpr (REAL) T::store(tile, j0 + off[r], T::template row_real<D>(M + r * D, v));
+      else T::store(tile, j0 + off[r], T::template row<D>(M + r * D, v));
+    }
   }
 }
 
@@ -131,6 +149,11 @@ __device__ __forceinline__ void apply_tile_op(typename T::S* tile, int L, const 
         tile[ja] = tile[jb];
         tile[jb] = va;
       }
+      break;
+    }
+    case GK_REAL: {
+      if (op.k == 1) apply_dense_tile<T, 1, true>(tile, L, op, M);
+      else apply_dense_tile<T, 2, true>(tile, L, op, M);
       break;
     }
     default: {

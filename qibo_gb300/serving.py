@@ -252,8 +252,14 @@ class _Flight:
 
 class Server:
     def __init__(self, budget_bytes: Optional[int] = None, nslots: int = 16, batch_max: int = 256,
-                 use_graphs: bool = True, one_at_a_time: bool = False, fuse_min_qubits: int = 16):
+                 use_graphs: bool = True, one_at_a_time: bool = False, fuse_min_qubits: int = 16,
+                 keep_states: bool = True):
+        """``keep_states=False``: state outputs still reach the host (pinned
+        buffers) but are dropped there instead of being kept in each
+        request's ``result``, so that long streams of large states fit in
+        host memory."""
         self.rt = Runtime.get()
+        self.keep_states = keep_states
         self.lib = self.rt.lib
         free, total = self.rt.mem_info()
         self.pool = DevicePool(self.rt, budget_bytes or int(free * 0.85))
@@ -402,7 +408,8 @@ class Server:
         for r, buf, nbytes in fl.hostbufs:
             view = buf[:nbytes]
             if r.output == "state":
-                r.result = view.view(np.complex128 if r.dtype == "complex128" else np.complex64).copy()
+                r.result = (view.view(np.complex128 if r.dtype == "complex128" else np.complex64).copy()
+                            if self.keep_states else None)
             elif r.output == "shots":
                 r.result = view.view(np.int64).copy()
             else:
