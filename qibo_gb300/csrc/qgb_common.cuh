@@ -117,6 +117,18 @@ __device__ __forceinline__ DFAcc df_add2(DFAcc s, float p, float e) {  // s + (p
   return r;
 }
 
+// a + b and a - b of double-float values (error-free sum of the heads, the
+// tails added, renormalised)
+__device__ __forceinline__ DFAcc df_plus(DFAcc a, DFAcc b) {
+  const float t = a.hi + b.hi;
+  const float bp = t - a.hi;
+  const float err = (a.hi - (t - bp)) + (b.hi - bp);
+  const float lo = (a.lo + b.lo) + err;
+  const float h = t + lo;
+  return DFAcc{h, lo - (h - t)};
+}
+__device__ __forceinline__ DFAcc df_minus(DFAcc a, DFAcc b) { return df_plus(a, DFAcc{-b.hi, -b.lo}); }
+
 // x = hi + lo (+ a remainder below 2^-47 |x|) as floats, with integer
 // operations and one integer-to-float conversion; valid for 2^-60 <= |x| <
 // 2^60 (false otherwise)
@@ -157,6 +169,11 @@ struct TC64 {
     return df_add2(s, py, fmaf(a.y, a.y, -py));
   }
   __device__ static double acc_value(Acc s) { return f2d_exact(s.hi) + f2d_exact(s.lo); }
+  // |a|^2 as a double-float (the squares split exactly)
+  __device__ static DFAcc abs2_df(V a) {
+    const float px = a.x * a.x, py = a.y * a.y;
+    return df_add2(DFAcc{px, fmaf(a.x, a.x, -px)}, py, fmaf(a.y, a.y, -py));
+  }
   // acc + |a|^2 as two FMAs (two FP64 operations instead of three)
   __device__ static double acc2(double acc, V a) {
     const double x = f2d_exact(a.x), y = f2d_exact(a.y);
@@ -211,6 +228,26 @@ struct TC128 {
     return s;
   }
   __device__ static double acc_value(Acc s) { return s.d + (f2d_exact(s.f.hi) + f2d_exact(s.f.lo)); }
+  // |a|^2 as a double-float: split parts squared on the FP32 pipe; a part
+  // of 2^60 or more goes through one FP64 square, one below 2^-60 adds
+  // less than 2^-120
+  __device__ static DFAcc abs2_df(V a) {
+    float xh, xl, yh, yl;
+    DFAcc r{0.f, 0.f};
+    if (d_split(a.x, &xh, &xl)) {
+      const float p = xh * xh;
+      r = df_add2(r, p, fmaf(2.f * xh + xl, xl, fmaf(xh, xh, -p)));
+    } else if (fabs(a.x) >= 0x1p60) {
+      r = df_add2(r, (float)(a.x * a.x), 0.f);
+    }
+    if (d_split(a.y, &yh, &yl)) {
+      const float p = yh * yh;
+      r = df_add2(r, p, fmaf(2.f * yh + yl, yl, fmaf(yh, yh, -p)));
+    } else if (fabs(a.y) >= 0x1p60) {
+      r = df_add2(r, (float)(a.y * a.y), 0.f);
+    }
+    return r;
+  }
   __device__ static double fma_d(double a, double b, double c) { return ::fma(a, b, c); }
   __device__ static V scale(V a, double s) { return make_double2(a.x * s, a.y * s); }
   __device__ static V neg(V a) { return make_double2(-a.x, -a.y); }

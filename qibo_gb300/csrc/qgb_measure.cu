@@ -570,6 +570,7 @@ struct TermSet {
   int nterms;
   u64 zmask[QGB_TERMS_PER_LAUNCH];   // amplitude-index bit masks
   double coef[QGB_TERMS_PER_LAUNCH]; // diagonal: c_t; flip: c_t f_t (see k_expect_flip)
+  float chi[QGB_TERMS_PER_LAUNCH], clo[QGB_TERMS_PER_LAUNCH];  // coef as a double-float
   // diagonal terms on 2^10 amplitudes or more: terms sorted by m = index
   // bits 5..9 of their mask, [mstart[m], mstart[m+1]) having that m
   uint32_t mused;
@@ -596,49 +597,56 @@ __global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// The same on runs of 2^10 amplitudes, one per warp: lane l takes amplitudes
-// base + l + 32 k, k < 32 (coalesced), so k spans index bits 5..9.  With
-// p_k = |psi|^2 and S the Walsh-Hadamard transform of p over k
-// (S[m] = sum_k (-1)^popc(k & m) p_k, five butterfly stages), term t adds
-// c_t (-1)^popc(base & z_t) S[m_t] for the run, m_t = index bits 5..9 of
-// z_t: about 8 FP64 operations per amplitude whatever the number of terms,
-// against one per term and amplitude (GB300's FP64 pipe, not HBM, bounds
-// these reductions).
-template <typename T>
+// The same on runs of 2^(5+WB) amplitudes, one per warp: lane l takes
+// amplitudes base + l + 32 k, k < 2^WB (coalesced), so k spans index bits
+// 5..4+WB.  With p_k = |psi|^2 and S the Walsh-Hadamard transform of p over
+// k (S[m] = sum_k (-1)^popc(k & m) p_k, WB butterfly stages), term t adds
+// c_t (-1)^popc(base & z_t) S[m_t] for the run, m_t = index bits 5..4+WB of
+// z_t: a cost per amplitude independent of the number of terms, against one
+// per term and amplitude.  Everything is double-float on the FP32 pipe
+// (about 48 bits; GB300's FP64 pipe would bound the pass otherwise): the
+// squares (split exactly), the butterflies, each run's signed coefficient
+// sums and their products with S; each thread's partial becomes one double.
+template <typename T, int WB>
 __global__ void __launch_bounds__(256) k_expect_diag_wht(const typename T::S* __restrict__ psi, i64 nruns,
                                                          const __grid_constant__ TermSet ts,
                                                          double* __restrict__ part) {
+  constexpr int K = 1 << WB;
   const int lane = threadIdx.x & 31;
   const i64 warp = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
   const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
+  DFAcc acc{0.f, 0.f};
   for (i64 w = warp; w < nruns; w += nwarps) {
-    const i64 base = (w << 10) | lane;
-    double p[32];
+    const i64 base = (w << (5 + WB)) | lane;
+    DFAcc p[K];
 #pragma unroll
-    for (int k = 0; k < 32; ++k) p[k] = T::abs2(T::load(psi, base | ((i64)k << 5)));
+    for (int k = 0; k < K; ++k) p[k] = T::abs2_df(T::load(psi, base | ((i64)k << 5)));
 #pragma unroll
-    for (int h = 1; h < 32; h <<= 1) {
+    for (int h = 1; h < K; h <<= 1) {
 #pragma unroll
-      for (int k = 0; k < 32; ++k) {
+      for (int k = 0; k < K; ++k) {
         if ((k & h) == 0) {
-          const double a = p[k], b = p[k | h];
-          p[k] = a + b;
-          p[k | h] = a - b;
+          const DFAcc a = p[k], b = p[k | h];
+          p[k] = df_plus(a, b);
+          p[k | h] = df_minus(a, b);
         }
       }
     }
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
+    for (int m = 0; m < K; ++m) {
       if (!((ts.mused >> m) & 1)) continue;
-      double cm = 0.0;
-      for (int t = ts.mstart[m]; t < ts.mstart[m + 1]; ++t)
-        cm += (__popcll((u64)base & ts.zmask[t]) & 1) ? -ts.coef[t] : ts.coef[t];
-      acc = fma(cm, p[m], acc);
+      DFAcc cm{0.f, 0.f};
+      for (int t = ts.mstart[m]; t < ts.mstart[m + 1]; ++t) {
+        const bool odd = __popcll((u64)base & ts.zmask[t]) & 1;
+        cm = df_plus(cm, odd ? DFAcc{-ts.chi[t], -ts.clo[t]} : DFAcc{ts.chi[t], ts.clo[t]});
+      }
+      // acc += cm * S[m]: the product of the heads split exactly, the cross terms added
+      const float ph = cm.hi * p[m].hi;
+      acc = df_add2(acc, ph, fmaf(cm.hi, p[m].hi, -ph) + fmaf(cm.hi, p[m].lo, cm.lo * p[m].hi));
     }
   }
-  acc = block_sum256(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  const double sum = block_sum256(f2d_exact(acc.hi) + f2d_exact(acc.lo));
+  if (threadIdx.x == 0) part[blockIdx.x] = sum;
 }
 
 // Terms sharing flip mask x (highest set bit hb): for each pair (i, j = i^x)
@@ -655,6 +663,32 @@ __global__ void __launch_bounds__(256) k_expect_flip(const typename T::S* __rest
   double acc = 0.0;
   const i64 stride = (i64)gridDim.x * blockDim.x;
   const i64 low = ((i64)1 << hb) - 1;
+  if constexpr (T::kind == QGB_C64) {
+    if (ts.nterms == 1) {
+      // complex64, one term: the sign folded into a, the two products of
+      // Re or Im of conj(a) b split exactly and summed in a double-float
+      // partial (the FP32 pipe), times the coefficient once per thread
+      DFAcc d{0.f, 0.f};
+      for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < npairs; t += stride) {
+        const i64 i = ((t >> hb) << (hb + 1)) | (t & low);
+        const float2 a = psi[i], b = psi[i ^ (i64)xmask];
+        const bool odd = __popcll((u64)i & ts.zmask[0]) & 1;
+        const float ax = odd ? -a.x : a.x, ay = odd ? -a.y : a.y;
+        if (ts.any_im) {  // ax by - ay bx
+          const float q1 = ax * b.y, q2 = ay * b.x;
+          d = df_add2(d, q1, fmaf(ax, b.y, -q1));
+          d = df_add2(d, -q2, -fmaf(ay, b.x, -q2));
+        } else {  // ax bx + ay by
+          const float q1 = ax * b.x, q2 = ay * b.y;
+          d = df_add2(d, q1, fmaf(ax, b.x, -q1));
+          d = df_add2(d, q2, fmaf(ay, b.y, -q2));
+        }
+      }
+      const double sum = block_sum256(ts.coef[0] * (f2d_exact(d.hi) + f2d_exact(d.lo)));
+      if (threadIdx.x == 0) part[blockIdx.x] = sum;
+      return;
+    }
+  }
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < npairs; t += stride) {
     const i64 i = ((t >> hb) << (hb + 1)) | (t & low);
     const i64 j = i ^ (i64)xmask;
@@ -731,11 +765,13 @@ int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t*
     memset(&ts, 0, sizeof(ts));
     ts.nterms = (int)g.terms.size();
     const u64 x = to_index_mask(g.x, n);
-    const bool wht = x == 0 && n >= 10;
+    constexpr int WB = 4;  // transform bits of k_expect_diag_wht
+    constexpr int WK = 1 << WB;
+    const bool wht = x == 0 && n >= 5 + WB;
     std::vector<int> order(g.terms.begin(), g.terms.end());
-    if (wht)  // diagonal terms by their index bits 5..9
+    if (wht)  // diagonal terms by their index bits 5..4+WB
       std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
-        return ((to_index_mask(zmask[p], n) >> 5) & 31) < ((to_index_mask(zmask[q], n) >> 5) & 31);
+        return ((to_index_mask(zmask[p], n) >> 5) & (WK - 1)) < ((to_index_mask(zmask[q], n) >> 5) & (WK - 1));
       });
     for (int k = 0; k < ts.nterms; ++k) {
       const int t = order[k];
@@ -743,6 +779,8 @@ int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t*
       const int ny = __builtin_popcountll(z & to_index_mask(xmask[t], n));
       ts.zmask[k] = z;
       ts.coef[k] = coef[t];
+      ts.chi[k] = (float)coef[t];
+      ts.clo[k] = (float)(coef[t] - (double)ts.chi[k]);
       if (x != 0) {  // f = +2 for ny mod 4 in {0, 1}, -2 for {2, 3}; odd ny uses Im
         ts.coef[k] = coef[t] * ((ny & 3) < 2 ? 2.0 : -2.0);
         if (ny & 1) {
@@ -756,19 +794,19 @@ int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t*
     }
     if (wht) {
       int k = 0;
-      for (int m = 0; m < 32; ++m) {
+      for (int m = 0; m < WK; ++m) {
         ts.mstart[m] = k;
-        while (k < ts.nterms && (int)((ts.zmask[k] >> 5) & 31) == m) ++k;
+        while (k < ts.nterms && (int)((ts.zmask[k] >> 5) & (WK - 1)) == m) ++k;
         if (k > ts.mstart[m]) ts.mused |= 1u << m;
       }
-      ts.mstart[32] = k;
+      ts.mstart[WK] = k;
     }
     int blocks;
     if (wht) {
-      const i64 nruns = N >> 10;
+      const i64 nruns = N >> (5 + WB);
       grid_for(nruns * 32, 256, &blocks);
       blocks = std::min(blocks, kExpectBlocksCap);
-      k_expect_diag_wht<T><<<blocks, 256, 0, s>>>((const S*)state, nruns, ts, part + used);
+      k_expect_diag_wht<T, WB><<<blocks, 256, 0, s>>>((const S*)state, nruns, ts, part + used);
     } else if (x == 0) {
       grid_for(N, 256, &blocks);
       blocks = std::min(blocks, kExpectBlocksCap);

@@ -476,11 +476,13 @@ def test_pauli_strings_with_y_vs_oracle(backend):
 
 
 @pytest.mark.parametrize("n", [10, 14])
-@pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-5)])
+@pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-12)])
 def test_z_strings_vs_oracle(n, dtype, tol):
     """Diagonal terms through the Walsh-Hadamard kernel (2^10 amplitudes or
     more): 100 random Z strings, so two launches of at most 64 terms, with
-    masks on every index bit including bits 5..9 that the transform spans."""
+    masks on every index bit including bits 5..9 that the transform spans.
+    The transform runs in double-float, so complex64 states too match the
+    exact value of their stored amplitudes to 1e-12."""
     from qibo_gb300.backend import GB300Backend
     from qibo_gb300.device import DeviceState
     from qibo_gb300.engine import pauli_masks
@@ -499,6 +501,31 @@ def test_z_strings_vs_oracle(n, dtype, tol):
     want = ref.exp_value_observable_symbolic(np.asarray(st).astype(np.complex128), terms, qubits, coefs, n)
     xs, zs = zip(*[pauli_masks(t, q) for t, q in zip(terms, qubits)])
     assert abs(b.engine_gb.expect_pauli(st, xs, zs, coefs) - want) < tol
+
+
+@pytest.mark.parametrize("n", [12, 18])
+def test_single_term_flips_complex64(n):
+    """One X or Y term per flip mask (the transverse-field terms of TFIM),
+    complex64: the double-float pair kernel against the exact value of the
+    stored amplitudes, to 1e-12."""
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+    from qibo_gb300.engine import pauli_masks
+
+    b = GB300Backend("complex64")
+    psi = rand_state(n, 77).astype(np.complex64)
+    rng = np.random.default_rng(12)
+    terms, qubits, coefs = [], [], []
+    for q in range(n):
+        f = "X" if q % 3 else "Y"
+        extra = [] if q % 2 else [int((q + 5) % n)]
+        terms.append(f + "Z" * len(extra))
+        qubits.append(tuple([q] + extra))
+        coefs.append(float(rng.normal()))
+    st = DeviceState.from_numpy(psi)
+    want = ref.exp_value_observable_symbolic(psi.astype(np.complex128), terms, qubits, coefs, n)
+    xs, zs = zip(*[pauli_masks(t, q) for t, q in zip(terms, qubits)])
+    assert abs(b.engine_gb.expect_pauli(st, xs, zs, coefs) - want) < 1e-12
 
 
 def test_dense_expectation_vs_oracle(backend):
