@@ -86,6 +86,42 @@ __device__ __forceinline__ void apply_dense_tile(typename T::S* tile, int L, con
     off[mm] = o;
   }
   const int groups = 1 << (L - K);
+  if constexpr (K <= 2 && sizeof(typename T::V) == 8) {
+    // complex64: two groups per step, so that their independent arithmetic
+    // chains interleave (measured 7 % faster passes; the double-float
+    // complex128 rows have too many live registers for it to pay)
+    for (int g = threadIdx.x; g < groups; g += 2 * blockDim.x) {
+      const int g1 = g + blockDim.x;
+      const bool has1 = g1 < groups;
+      int j0 = g, j1 = has1 ? g1 : g;
+#pragma unroll
+      for (int i = 0; i < K; ++i) {
+        j0 = ins0(j0, sorted[i]);
+        j1 = ins0(j1, sorted[i]);
+      }
+      const bool act0 = (j0 & op.lmask) == op.lmask, act1 = has1 && (j1 & op.lmask) == op.lmask;
+      typename T::V v0[D], v1[D];
+#pragma unroll
+      for (int mm = 0; mm < D; ++mm) {
+        v0[mm] = T::load(tile, j0 + off[mm]);
+        v1[mm] = T::load(tile, j1 + off[mm]);
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        typename T::V o0, o1;
+        if constexpr (REAL) {
+          o0 = T::template row_real<D>(M + r * D, v0);
+          o1 = T::template row_real<D>(M + r * D, v1);
+        } else {
+          o0 = T::template row<D>(M + r * D, v0);
+          o1 = T::template row<D>(M + r * D, v1);
+        }
+        if (act0) T::store(tile, j0 + off[r], o0);
+        if (act1) T::store(tile, j1 + off[r], o1);
+      }
+    }
+    return;
+  }
   for (int g = threadIdx.x; g < groups; g += blockDim.x) {
     int j0 = g;
 #pragma unroll
