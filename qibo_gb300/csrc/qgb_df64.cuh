@@ -89,10 +89,11 @@ __device__ __forceinline__ cdf cdf_mul(cdf x, cdf y) { return cdf_row<1>(&x, &y)
 // Split: hi = x with its mantissa truncated to 24 bits; the 29 remaining
 // mantissa bits r give lo = RN(r) * 2^(e - 1075), |lo| < ulp(hi), so
 // x - (hi + lo) is below 2^-47 |x| (for |x| >= 2^-100; below, lo is a
-// subnormal float and the error below 2^-149).  Integer operations, one
-// integer to float conversion and two multiplications by powers of two, on
-// every path: |x| < 2^-126 becomes 0, |x| >= 2^128 an infinity, NaN a NaN.
-__device__ __forceinline__ df df_split_int(double x) {
+// subnormal float and the error below 2^-149).  df_split_exact covers the
+// exponent fields E < 950 and E > 1150 with integer operations, one integer
+// to float conversion and two multiplications by powers of two: |x| <
+// 2^-126 becomes 0, |x| >= 2^128 an infinity, NaN a NaN.
+__device__ __forceinline__ df df_split_exact(double x) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const uint32_t h = (uint32_t)(u >> 32), l = (uint32_t)u;
   const uint32_t sign = h & 0x80000000u;
@@ -109,21 +110,50 @@ __device__ __forceinline__ df df_split_int(double x) {
   return {__uint_as_float(hib), lo};
 }
 
-// The join's widening: hi and lo come out of df_renorm, so each is a zero or
-// a normal float, except a lo below 2^-126, which read as normal errs by less
-// than 2^-125; infinities and NaNs keep exponent 2047.
-__device__ __forceinline__ double f2d_join(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-  const uint64_t de = e == 0xFFu ? 0x7FFull : (uint64_t)(e + 896u);
-  const uint64_t bits = (u << 1) == 0 ? 0ull : (de << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)(sign | bits));
+// The rare cases of the two conversions below, out of line: a call is a
+// branch the compiler cannot turn into predicated code on the common path.
+static __device__ __noinline__ df df_split_rare(double x) { return df_split_exact(x); }
+static __device__ __noinline__ double df_join_rare(float hi, float lo) { return (double)hi + (double)lo; }
+
+// The same split, shorter for 2^-73 <= |x| < 2^128 (the exponent field E
+// in [950, 1150]): hi's bits are bits 60..29 of x shifted left by 3 (the
+// top 23 fraction bits under the low 9 exponent bits), re-biased by
+// subtracting 0x180 from that 9-bit field modulo 2^9 (E - 896 = E mod 2^9 -
+// 384 modulo 2^9, sign restored); lo is the low 29 fraction bits as a
+// float times 2^(E - 1075), a normal float in this range.
+__device__ __forceinline__ df df_split_int(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const uint32_t h = (uint32_t)(u >> 32), l = (uint32_t)u;
+  const uint32_t E = (h >> 20) & 0x7FFu;
+  if (__builtin_expect(E - 950u > 200u, 0)) return df_split_rare(x);
+  const uint32_t w = __funnelshift_l(l, h, 3);
+  const uint32_t sign = h & 0x80000000u;
+  const uint32_t hib = ((w - 0xC0000000u) & 0x7FFFFFFFu) | sign;
+  const float lo = __uint2float_rn(l & 0x1FFFFFFFu) * __uint_as_float((E - 948u) << 23);
+  return {__uint_as_float(hib), __uint_as_float(__float_as_uint(lo) | sign)};
 }
 
-// hi + lo rounded once to an IEEE double: both widen exactly with integer
-// operations; the one FP64 addition rounds.
-__device__ __forceinline__ double df_join(df a) { return f2d_join(a.hi) + f2d_join(a.lo); }
+// hi + lo rounded once to an IEEE double (RN(hi + lo), as an FP64 addition
+// of the widened floats gives), without the FP64 pipe when hi is normal and
+// at least 2^-75, and the sum stays in hi's binade: hi widens by integer
+// operations, and lo, in units of the double's last place at hi's exponent
+// (one FP32 multiplication by 2^(179 - e) with hi's sign, exact), is rounded
+// to an integer (ties to even) and added to the widened bits.  The binade is
+// kept when that integer is below 2^29 in magnitude and, for hi a power of
+// two, not negative.  Other pairs (zeros, subnormals, |hi| < 2^-75,
+// infinities, NaNs, a lo at least as large as ulp(hi) after a cancellation)
+// take one FP64 addition.
+__device__ __forceinline__ double df_join(df a) {
+  const uint32_t uh = __float_as_uint(a.hi);
+  const uint32_t ex = uh & 0x7F800000u;
+  const float scale = __uint_as_float(((306u << 23) - ex) | (uh & 0x80000000u));
+  const float rf = a.lo * scale;
+  const bool fast = (ex - (52u << 23)) < (203u << 23) && fabsf(rf) < 536870912.0f &&
+                    ((uh & 0x7FFFFFu) != 0u || rf >= 0.f);
+  if (__builtin_expect(!fast, 0)) return df_join_rare(a.hi, a.lo);
+  const int64_t mag = ((int64_t)(uh & 0x7FFFFFFFu) << 29) + (int64_t)__float2int_rn(rf) + ((int64_t)896 << 52);
+  return __longlong_as_double((long long)((uint64_t)mag | ((uint64_t)(uh & 0x80000000u) << 32)));
+}
 
 __device__ __forceinline__ df df_add(df a, df b) {
   float s, e;
@@ -179,8 +209,8 @@ struct TC128F {
     c.im = df_split(im);
     return c;
   }
-  // tiles convert with integer operations (df_split_int) and one FP64
-  // addition per double on the way back (df_join)
+  // tiles convert with integer operations both ways (df_split_int,
+  // df_join)
   __device__ static V from_global(double2 v) {
     cdf c;
     c.re = df_split_int(v.x);

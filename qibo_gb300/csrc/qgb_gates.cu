@@ -86,22 +86,82 @@ __global__ void __launch_bounds__(256) k_1q_pairs(typename T::S* __restrict__ ps
   pairs_body<T>(psi, npairs, b, u00, u01, u10, u11);
 }
 
-// complex128 gate by gate, the two arithmetic pipes at once: the first nf64
-// warps of every block compute their pairs in IEEE FP64 (the FP64 pipe, 16
-// DFMA per pair), the others in double-float (FP32 and integer pipes).
-// Alone, the FP64 form is bound by GB300's FP64 rate and the double-float
-// form by instruction issue; sharing the pairs between them keeps both
-// pipes busy part of the time.  Which warp computes which pair does not depend on nf64, and
-// both forms are accurate to a few units in the last place of FP64.
+// complex128 gate by gate, the two arithmetic pipes at once: some warps
+// compute their pairs in IEEE FP64 (the FP64 pipe, 16 DFMA per pair), the
+// others in double-float (FP32 and integer pipes only).  Alone, the FP64
+// form is bound by GB300's FP64 rate and the double-float form by
+// instruction issue; sharing the pairs between them keeps both pipes busy.
+// A block has 1024 threads, one per SM: warp w issues from scheduler w mod 4
+// as the (w / 4)-th of that scheduler's eight warps, and the first nf64 of
+// each scheduler's eight take the FP64 form, so all four schedulers (each
+// with its own FP64 units) carry the same share.  Which warp computes which
+// pair does not depend on nf64, and both forms are accurate to a few units
+// in the last place of FP64.
+//
+// Loads go through a ring of MIX_STAGES slots per thread in shared memory,
+// filled by cp.async (16 bytes per copy, no registers held), MIX_STAGES - 1
+// steps ahead of the arithmetic: every thread reads back only its own
+// slots, after cp.async.wait_group has seen its own copies land, so no
+// barrier is needed.  A slot is refilled one step after it was read into
+// registers, and stores go straight from registers to the state.
+#define MIX_THREADS 1024
+#define MIX_STAGES 4
 struct Coef1q {
   cdf d[4];      // double-float u00, u01, u10, u11
   double2 e[4];  // the same in FP64
 };
 
-__global__ void __launch_bounds__(256) k_1q_pairs_mix(double2* __restrict__ psi, i64 npairs, int b, int nf64,
-                                                      const __grid_constant__ Coef1q u) {
-  if ((int)(threadIdx.x >> 5) < nf64) pairs_body<TC128>(psi, npairs, b, u.e[0], u.e[1], u.e[2], u.e[3]);
-  else pairs_body<DF128>(psi, npairs, b, u.d[0], u.d[1], u.d[2], u.d[3]);
+__device__ __forceinline__ bool mix_fp64_warp(int nf64) { return (int)(threadIdx.x >> 7) < nf64; }
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+extern __shared__ __align__(16) double2 mix_ring[];
+
+// pairs_body through the ring: slot k of a thread holds its pair's two
+// amplitudes at mix_ring[(2 k + h) MIX_THREADS + thread]
+template <typename T>
+__device__ __forceinline__ void pairs_ring_body(double2* __restrict__ psi, i64 npairs, int b, typename T::V u00,
+                                                typename T::V u01, typename T::V u10, typename T::V u11) {
+  const i64 stride = (i64)gridDim.x * MIX_THREADS;
+  const i64 lowmask = ((i64)1 << b) - 1, step = (i64)1 << b;
+  const i64 t0 = (i64)blockIdx.x * MIX_THREADS + threadIdx.x;
+  double2* const slot = mix_ring + threadIdx.x;
+  const auto fetch = [&](i64 t, int k) {
+    if (t < npairs) {
+      const i64 i0 = ((t >> b) << (b + 1)) | (t & lowmask);
+      cp_async16(slot + (2 * k) * MIX_THREADS, psi + i0);
+      cp_async16(slot + (2 * k + 1) * MIX_THREADS, psi + i0 + step);
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int k = 0; k < MIX_STAGES - 1; ++k) fetch(t0 + k * stride, k);
+  int k = 0;
+  for (i64 t = t0; t < npairs; t += stride) {
+    cp_async_wait<MIX_STAGES - 2>();  // slot k has landed
+    fetch(t + (MIX_STAGES - 1) * stride, k == 0 ? MIX_STAGES - 1 : k - 1);
+    const typename T::V a0 = T::load(slot, (2 * k) * MIX_THREADS), a1 = T::load(slot, (2 * k + 1) * MIX_THREADS);
+    const i64 i0 = ((t >> b) << (b + 1)) | (t & lowmask);
+    T::store(psi, i0, T::row2(u00, a0, u01, a1));
+    T::store(psi, i0 + step, T::row2(u10, a0, u11, a1));
+    k = k == MIX_STAGES - 1 ? 0 : k + 1;
+  }
+  cp_async_wait<0>();
+}
+
+__global__ void __launch_bounds__(MIX_THREADS) k_1q_pairs_mix(double2* __restrict__ psi, i64 npairs, int b,
+                                                              int nf64, const __grid_constant__ Coef1q u) {
+  if (mix_fp64_warp(nf64)) pairs_ring_body<TC128>(psi, npairs, b, u.e[0], u.e[1], u.e[2], u.e[3]);
+  else pairs_ring_body<DF128>(psi, npairs, b, u.d[0], u.d[1], u.d[2], u.d[3]);
 }
 
 template <typename V>
@@ -136,12 +196,20 @@ __device__ __forceinline__ void shfl_body(typename T::S* __restrict__ psi, i64 N
   const bool hi = (lane >> b) & 1;
   const typename T::V cs = hi ? u11 : u00;  // coefficient of own amplitude
   const typename T::V cp = hi ? u10 : u01;  // coefficient of the partner
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
-    // N is a multiple of 32 and stride is a multiple of 32: whole warps stay
-    // in the loop together, so the full-mask shuffle is safe.
-    typename T::V a = T::load(psi, i);
+  // two windows per step (i and i + stride) for two independent chains;
+  // N and stride are multiples of 32, so whole warps take the same branches
+  // and every full-mask shuffle sees all 32 lanes
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += 2 * stride) {
+    const i64 j = i + stride;
+    const bool has2 = j < N;
+    typename T::V a = T::load(psi, i), c;
+    if (has2) c = T::load(psi, j);
     typename T::V p = shfl_xor_v(a, 1 << b);
     T::store(psi, i, T::row2(cs, a, cp, p));
+    if (has2) {
+      typename T::V q = shfl_xor_v(c, 1 << b);
+      T::store(psi, j, T::row2(cs, c, cp, q));
+    }
   }
 }
 
@@ -152,12 +220,42 @@ __global__ void __launch_bounds__(256) k_1q_shfl(typename T::S* __restrict__ psi
   shfl_body<T>(psi, N, b, u00, u01, u10, u11);
 }
 
+// shfl_body through the ring (slot k of a thread: mix_ring[k MIX_THREADS +
+// thread]).  N and the stride are multiples of 32, so whole warps run the
+// same steps and every full-mask shuffle sees all 32 lanes.
+template <typename T>
+__device__ __forceinline__ void shfl_ring_body(double2* __restrict__ psi, i64 N, int b, typename T::V u00,
+                                               typename T::V u01, typename T::V u10, typename T::V u11) {
+  const i64 stride = (i64)gridDim.x * MIX_THREADS;
+  const bool hi = ((threadIdx.x & 31) >> b) & 1;
+  const typename T::V cs = hi ? u11 : u00;  // coefficient of own amplitude
+  const typename T::V cp = hi ? u10 : u01;  // coefficient of the partner
+  const i64 i0 = (i64)blockIdx.x * MIX_THREADS + threadIdx.x;
+  double2* const slot = mix_ring + threadIdx.x;
+  const auto fetch = [&](i64 i, int k) {
+    if (i < N) cp_async16(slot + k * MIX_THREADS, psi + i);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int k = 0; k < MIX_STAGES - 1; ++k) fetch(i0 + k * stride, k);
+  int k = 0;
+  for (i64 i = i0; i < N; i += stride) {
+    cp_async_wait<MIX_STAGES - 2>();
+    fetch(i + (MIX_STAGES - 1) * stride, k == 0 ? MIX_STAGES - 1 : k - 1);
+    const typename T::V a = T::load(slot, k * MIX_THREADS);
+    const typename T::V p = shfl_xor_v(a, 1 << b);
+    T::store(psi, i, T::row2(cs, a, cp, p));
+    k = k == MIX_STAGES - 1 ? 0 : k + 1;
+  }
+  cp_async_wait<0>();
+}
+
 // k_1q_shfl with the pipes shared as in k_1q_pairs_mix (warp-uniform split,
 // so every shuffle still sees a whole warp)
-__global__ void __launch_bounds__(256) k_1q_shfl_mix(double2* __restrict__ psi, i64 N, int b, int nf64,
-                                                     const __grid_constant__ Coef1q u) {
-  if ((int)(threadIdx.x >> 5) < nf64) shfl_body<TC128>(psi, N, b, u.e[0], u.e[1], u.e[2], u.e[3]);
-  else shfl_body<DF128>(psi, N, b, u.d[0], u.d[1], u.d[2], u.d[3]);
+__global__ void __launch_bounds__(MIX_THREADS) k_1q_shfl_mix(double2* __restrict__ psi, i64 N, int b, int nf64,
+                                                             const __grid_constant__ Coef1q u) {
+  if (mix_fp64_warp(nf64)) shfl_ring_body<TC128>(psi, N, b, u.e[0], u.e[1], u.e[2], u.e[3]);
+  else shfl_ring_body<DF128>(psi, N, b, u.d[0], u.d[1], u.d[2], u.d[3]);
 }
 
 // multiply ``phase`` into every amplitude whose ``mask`` bits are all 1
@@ -268,12 +366,12 @@ i64 mask_of(const std::vector<int>& bits) {
   return m;
 }
 
-// Warps per 256-thread block that compute dense 1-qubit complex128 gates in
-// IEEE FP64 while the rest use double-float (k_1q_pairs_mix); the
+// Warps of every eight on a scheduler that compute dense 1-qubit complex128
+// gates in IEEE FP64 while the rest use double-float (k_1q_pairs_mix); the
 // QIBO_GB300_DF_FP64_WARPS variable (0-8) overrides it for comparisons.
-// Measured at n=30 (one pass, 34.4 GB): 0/8 8.30 ms, 2/8 7.56 ms, 3/8
-// 8.38 ms, 4/8 9.51 ms, 8/8 14.41 ms.  The pipes overlap only in part: with
-// 3/8 in FP64 each alone would take about 5.4 ms.
+// Measured at n=30 (one pass, 34.4 GB), target qubit 0 / n-1: 0 of 8
+// 6.49 / 6.89 ms, 2 of 8 5.36 / 5.53 ms, 3 of 8 6.41 / 5.79 ms, 4 of 8
+// 8.20 / 7.53 ms.
 int df_fp64_warps() {
   const char* v = getenv("QIBO_GB300_DF_FP64_WARPS");
   if (v && *v) {
@@ -312,17 +410,22 @@ int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
         cu.e[m] = TC128::coef(M[m].real(), M[m].imag());
       }
       const int nf64 = df_fp64_warps();
-      int blocks;
+      // one block per SM, each looping over its share
+      const auto mix_blocks = [](i64 items) {
+        const i64 b = (items + MIX_THREADS - 1) / MIX_THREADS;
+        return (int)std::max<i64>(1, std::min<i64>(b, qgb_num_sms()));
+      };
+      const int ring = MIX_STAGES * MIX_THREADS * (int)sizeof(double2);  // per amplitude of a step
       if (b < 5 && n >= 5) {
         const i64 N = (i64)1 << n;
-        grid_for(N, 256, &blocks);
-        k_1q_shfl_mix<<<blocks, 256, 0, s>>>((double2*)state, N, b, nf64, cu);
+        if (int st = qgb_func_smem((const void*)k_1q_shfl_mix, ring)) return st;
+        k_1q_shfl_mix<<<mix_blocks(N), MIX_THREADS, ring, s>>>((double2*)state, N, b, nf64, cu);
         QGB_LAUNCH_CHECK("k_1q_shfl_mix");
         return QGB_OK;
       }
       if (b >= 5) {
-        grid_for((ngroups + 1) / 2, 256, &blocks);
-        k_1q_pairs_mix<<<blocks, 256, 0, s>>>((double2*)state, ngroups, b, nf64, cu);
+        if (int st = qgb_func_smem((const void*)k_1q_pairs_mix, 2 * ring)) return st;
+        k_1q_pairs_mix<<<mix_blocks(ngroups), MIX_THREADS, 2 * ring, s>>>((double2*)state, ngroups, b, nf64, cu);
         QGB_LAUNCH_CHECK("k_1q_pairs_mix");
         return QGB_OK;
       }
