@@ -455,9 +455,9 @@ def complex64_legs(args, n, circ, descs, state, backend, ev, ndense, ncz, runs=8
                 "ms": ms_df, "GB/s": g128 / (ms_df * 1e-3) / 1e9,
                 "frac_of_hbm_peak": g128 / (ms_df * 1e-3) / 1e9 / measured_peaks().get("hbm_gbs", 6800.0),
                 "infidelity_vs_per_gate_fp64": inf_df,
-                "note": "one pass per gate; dense 1-qubit gates with 2 of 8 warps in IEEE FP64 and 6 in "
-                        "double-float (the doubles split and joined with integer operations), dense 2-qubit gates "
-                        "in double-float; CZ by sign flips"},
+                "note": "one pass per gate; dense 1-qubit gates with 2 of every 8 warps per scheduler in IEEE "
+                        "FP64 and 6 in double-float, loads staged through shared memory by cp.async; dense "
+                        "2-qubit gates in double-float; CZ by sign flips"},
             "c128_fused_infidelity_vs_per_gate_fp64": inf_128,
             "fused_tc_speedup_vs_c128_per_gate": ms_g / p50}
 
@@ -1004,7 +1004,7 @@ def run_kernels(args):
             (f"dense 1q gate by gate{df}, qubit n-1", "k_1q_shfl_mix" if df else "k_1q_shfl", 2 * N * S,
              circuit_gate(n - 1)),
         ]
-        if dtype == "complex128":  # the share of FP64 warps per 8-warp block
+        if dtype == "complex128":  # the share of FP64 warps among each scheduler's 8
             for w in (0, 1, 2, 3, 4, 8):
                 calls.append((f"dense 1q gate by gate, qubit 0, {w}/8 warps in FP64", "k_1q_pairs_mix", 2 * N * S,
                               with_fp64_warps(w, circuit_gate(0))))

@@ -155,6 +155,21 @@ __device__ __forceinline__ double df_join(df a) {
   return __longlong_as_double((long long)((uint64_t)mag | ((uint64_t)(uh & 0x80000000u) << 32)));
 }
 
+// hi + lo rounded once to an IEEE double by one FP64 addition, the two
+// floats widened with integer operations (hi and lo come out of df_renorm,
+// so each is a zero or a normal float, except a lo below 2^-126, which read
+// as normal errs by less than 2^-125; infinities and NaNs keep exponent
+// 2047).  Shared-memory passes use this form: their FP64 pipe is idle.
+__device__ __forceinline__ double f2d_join(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  const uint64_t de = e == 0xFFu ? 0x7FFull : (uint64_t)(e + 896u);
+  const uint64_t bits = (u << 1) == 0 ? 0ull : (de << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)(sign | bits));
+}
+__device__ __forceinline__ double df_join_fp64(df a) { return f2d_join(a.hi) + f2d_join(a.lo); }
+
 __device__ __forceinline__ df df_add(df a, df b) {
   float s, e;
   two_sum(a.hi, b.hi, s, e);
@@ -209,15 +224,16 @@ struct TC128F {
     c.im = df_split(im);
     return c;
   }
-  // tiles convert with integer operations both ways (df_split_int,
-  // df_join)
+  // tiles convert with integer operations (df_split_exact) and one FP64
+  // addition per double on the way back (df_join_fp64): branch-free forms,
+  // measured faster inside the passes than the per-gate kernels' fast paths
   __device__ static V from_global(double2 v) {
     cdf c;
-    c.re = df_split_int(v.x);
-    c.im = df_split_int(v.y);
+    c.re = df_split_exact(v.x);
+    c.im = df_split_exact(v.y);
     return c;
   }
-  __device__ static double2 to_global(V v) { return make_double2(df_join(v.re), df_join(v.im)); }
+  __device__ static double2 to_global(V v) { return make_double2(df_join_fp64(v.re), df_join_fp64(v.im)); }
   __device__ static V load(const S* p, int i) { return p[i]; }
   __device__ static void store(S* p, int i, V v) { p[i] = v; }
   __device__ static V mul(V a, V b) { return cdf_mul(a, b); }
