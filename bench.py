@@ -988,6 +988,9 @@ def run_kernels(args):
             return lambda: check(lib.qgb_apply_circuit(st.ptr, n, code, one.ctypes.data_as(C.POINTER(_lib.QgbOp)), 1,
                                                        c1.ctypes.data_as(_lib.dp), 0, s))
 
+        def circuit_desc(desc):  # any gate (qubits, controls, matrix) through qgb_apply_circuit, gate by gate
+            return lambda: eng.apply_many(st, [desc])
+
         def with_fp64_warps(w, fn):  # QIBO_GB300_DF_FP64_WARPS around one call
             def run():
                 os.environ["QIBO_GB300_DF_FP64_WARPS"] = str(w)
@@ -1003,6 +1006,14 @@ def run_kernels(args):
              circuit_gate(0)),
             (f"dense 1q gate by gate{df}, qubit n-1", "k_1q_shfl_mix" if df else "k_1q_shfl", 2 * N * S,
              circuit_gate(n - 1)),
+        ]
+        u2m = u2.view(np.complex128).reshape(4, 4)
+        u1m = u1.view(np.complex128).reshape(2, 2)
+        calls += [
+            (f"dense 2q gate by gate{df}, qubits 3, n-5", "k_dense_mix<2>" if df else "k_dense<2>", 2 * N * S,
+             circuit_desc(((3, n - 5), (), u2m))),
+            (f"U3 gate by gate{df} on qubit 5 controlled by qubits 1, 2", "k_dense_mix<1>" if df else "k_dense<1>",
+             2 * N * S // 4, circuit_desc(((5,), (1, 2), u1m))),
         ]
         if dtype == "complex128":  # the share of FP64 warps among each scheduler's 8
             for w in (0, 1, 2, 3, 4, 8):

@@ -146,7 +146,7 @@ struct AdjMats {
 // one parametrised gate of the reverse sweep (see the file comment)
 template <typename T, int K>
 __global__ void __launch_bounds__(256) k_adjoint_step(typename T::S* __restrict__ psi, typename T::S* __restrict__ lam,
-                                                      i64 ngroups, BitInsert bi, i64 cmask, Offs5 off, int nder,
+                                                      i64 ngroups, const __grid_constant__ BitInsert bi, i64 cmask, Offs5 off, int nder,
                                                       const __grid_constant__ AdjMats<T, K> M, double* __restrict__ part,
                                                       int part_stride) {
   constexpr int D = 1 << K;

@@ -164,6 +164,75 @@ __global__ void __launch_bounds__(MIX_THREADS) k_1q_pairs_mix(double2* __restric
   else pairs_ring_body<DF128>(psi, npairs, b, u.d[0], u.d[1], u.d[2], u.d[3]);
 }
 
+// Dense complex128 gates of 1 qubit with controls or of 2 qubits, gate by
+// gate, with the FP64 / double-float warp split and the load ring of
+// k_1q_pairs_mix: a thread's group of D = 2^K amplitudes (base
+// insert_zeros(t) | cmask, offsets off.o) sits in ring slots
+// mix_ring[(k D + j) MIX_THREADS + thread], DENSE_STAGES(K) steps deep (the
+// 2-qubit ring takes 192 KB).  An output row is a complex multiply-add chain
+// in IEEE FP64, or one error-free dot product of 2 D terms per real output in
+// double-float.
+template <int K>
+struct CoefDense {
+  cdf d[1 << K][1 << K];      // double-float rows
+  double2 e[1 << K][1 << K];  // the same in FP64
+};
+#define DENSE_STAGES(K) ((K) == 2 ? 3 : MIX_STAGES)
+
+template <typename T, int D>
+__device__ __forceinline__ typename T::V dense_row(const typename T::V* u, const typename T::V* a) {
+  if constexpr (std::is_same<T, DF128>::value) {
+    return cdf_row<D>(u, a);
+  } else {
+    typename T::V acc = T::mul(u[0], a[0]);
+#pragma unroll
+    for (int c = 1; c < D; ++c) acc = T::fma(u[c], a[c], acc);
+    return acc;
+  }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void dense_ring_body(double2* __restrict__ psi, i64 ngroups, const BitInsert& bi,
+                                                i64 cmask, const Offs<K>& off,
+                                                const typename T::V (&m)[1 << K][1 << K]) {
+  constexpr int D = 1 << K, S = DENSE_STAGES(K);
+  const i64 stride = (i64)gridDim.x * MIX_THREADS;
+  const i64 t0 = (i64)blockIdx.x * MIX_THREADS + threadIdx.x;
+  double2* const slot = mix_ring + threadIdx.x;
+  const auto fetch = [&](i64 t, int k) {
+    if (t < ngroups) {
+      const i64 base = insert_zeros(t, bi) | cmask;
+#pragma unroll
+      for (int j = 0; j < D; ++j) cp_async16(slot + (k * D + j) * MIX_THREADS, psi + base + off.o[j]);
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int k = 0; k < S - 1; ++k) fetch(t0 + k * stride, k);
+  int k = 0;
+  for (i64 t = t0; t < ngroups; t += stride) {
+    cp_async_wait<S - 2>();  // slot k has landed
+    fetch(t + (S - 1) * stride, k == 0 ? S - 1 : k - 1);
+    typename T::V v[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) v[j] = T::load(slot, (k * D + j) * MIX_THREADS);
+    const i64 base = insert_zeros(t, bi) | cmask;
+#pragma unroll
+    for (int r = 0; r < D; ++r) T::store(psi, base + off.o[r], dense_row<T, D>(m[r], v));
+    k = k == S - 1 ? 0 : k + 1;
+  }
+  cp_async_wait<0>();
+}
+
+template <int K>
+__global__ void __launch_bounds__(MIX_THREADS) k_dense_mix(double2* __restrict__ psi, i64 ngroups,
+                                                           const __grid_constant__ BitInsert bi, i64 cmask,
+                                                           const __grid_constant__ Offs<K> off, int nf64,
+                                                           const __grid_constant__ CoefDense<K> u) {
+  if (mix_fp64_warp(nf64)) dense_ring_body<TC128, K>(psi, ngroups, bi, cmask, off, u.e);
+  else dense_ring_body<DF128, K>(psi, ngroups, bi, cmask, off, u.d);
+}
+
 template <typename V>
 __device__ __forceinline__ V shfl_xor_v(V v, int mask);
 template <>
@@ -196,19 +265,22 @@ __device__ __forceinline__ void shfl_body(typename T::S* __restrict__ psi, i64 N
   const bool hi = (lane >> b) & 1;
   const typename T::V cs = hi ? u11 : u00;  // coefficient of own amplitude
   const typename T::V cp = hi ? u10 : u01;  // coefficient of the partner
-  // two windows per step (i and i + stride) for two independent chains;
+  // W windows per step (i, i + stride, ...) for W independent chains and W
+  // loads in flight per thread (4 for 8-byte amplitudes, 2 for 16-byte);
   // N and stride are multiples of 32, so whole warps take the same branches
   // and every full-mask shuffle sees all 32 lanes
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += 2 * stride) {
-    const i64 j = i + stride;
-    const bool has2 = j < N;
-    typename T::V a = T::load(psi, i), c;
-    if (has2) c = T::load(psi, j);
-    typename T::V p = shfl_xor_v(a, 1 << b);
-    T::store(psi, i, T::row2(cs, a, cp, p));
-    if (has2) {
-      typename T::V q = shfl_xor_v(c, 1 << b);
-      T::store(psi, j, T::row2(cs, c, cp, q));
+  constexpr int W = sizeof(typename T::S) == 8 ? 4 : 2;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += W * stride) {
+    typename T::V a[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+      if (i + w * stride < N) a[w] = T::load(psi, i + w * stride);
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      if (i + w * stride < N) {
+        const typename T::V p = shfl_xor_v(a[w], 1 << b);
+        T::store(psi, i + w * stride, T::row2(cs, a[w], cp, p));
+      }
     }
   }
 }
@@ -260,7 +332,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_1q_shfl_mix(double2* __restrict
 
 // multiply ``phase`` into every amplitude whose ``mask`` bits are all 1
 template <typename T>
-__global__ void __launch_bounds__(256) k_phase(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+__global__ void __launch_bounds__(256) k_phase(typename T::S* __restrict__ psi, i64 count, const __grid_constant__ BitInsert bi,
                                                i64 mask, typename T::V phase) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
@@ -278,25 +350,36 @@ __device__ __forceinline__ double flip_sign(double x) {
 __device__ __forceinline__ float flip_sign(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000u); }
 
 template <typename S>
-__global__ void __launch_bounds__(256) k_phase_unit(S* __restrict__ psi, i64 count, BitInsert bi, i64 mask,
+__global__ void __launch_bounds__(256) k_phase_unit(S* __restrict__ psi, i64 count, const __grid_constant__ BitInsert bi, i64 mask,
                                                     int mode) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
-    const i64 i = insert_zeros(t, bi) | mask;
-    S v = psi[i];
-    if (mode == 1) {  // -1
-      v.x = flip_sign(v.x);
-      v.y = flip_sign(v.y);
-    } else if (mode == 2) {  // i: (x, y) -> (-y, x)
-      const auto x = v.x;
-      v.x = flip_sign(v.y);
-      v.y = x;
-    } else {  // -i: (x, y) -> (y, -x)
-      const auto x = v.x;
-      v.x = v.y;
-      v.y = flip_sign(x);
+  // W amplitudes per step for W loads in flight (4 of 8 bytes, 2 of 16)
+  constexpr int W = sizeof(S) == 8 ? 4 : 2;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += W * stride) {
+    i64 idx[W];
+    S v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      idx[w] = t + w * stride < count ? insert_zeros(t + w * stride, bi) | mask : -1;
+      if (idx[w] >= 0) v[w] = psi[idx[w]];
     }
-    psi[i] = v;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      if (idx[w] < 0) continue;
+      if (mode == 1) {  // -1
+        v[w].x = flip_sign(v[w].x);
+        v[w].y = flip_sign(v[w].y);
+      } else if (mode == 2) {  // i: (x, y) -> (-y, x)
+        const auto x = v[w].x;
+        v[w].x = flip_sign(v[w].y);
+        v[w].y = x;
+      } else {  // -i: (x, y) -> (y, -x)
+        const auto x = v[w].x;
+        v[w].x = v[w].y;
+        v[w].y = flip_sign(x);
+      }
+      psi[idx[w]] = v[w];
+    }
   }
 }
 
@@ -305,7 +388,7 @@ template <typename T>
 struct DiagVec { typename T::V d[32]; };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_diagk(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+__global__ void __launch_bounds__(256) k_diagk(typename T::S* __restrict__ psi, i64 count, const __grid_constant__ BitInsert bi,
                                                i64 cmask, int k, Offs<QGB_MAX_K> tbit, DiagVec<T> D) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
@@ -318,7 +401,7 @@ __global__ void __launch_bounds__(256) k_diagk(typename T::S* __restrict__ psi, 
 
 // X-like 1-qubit gate [[0, a], [b, 0]] with controls: new0 = a*old1, new1 = b*old0
 template <typename T>
-__global__ void __launch_bounds__(256) k_xlike(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+__global__ void __launch_bounds__(256) k_xlike(typename T::S* __restrict__ psi, i64 count, const __grid_constant__ BitInsert bi,
                                                i64 cmask, i64 tstep, typename T::V a, typename T::V b,
                                                int plain) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
@@ -337,7 +420,7 @@ __global__ void __launch_bounds__(256) k_xlike(typename T::S* __restrict__ psi, 
 
 // SWAP of bits (a, b) with controls: exchanges |..0..1..> and |..1..0..>
 template <typename T>
-__global__ void __launch_bounds__(256) k_swap(typename T::S* __restrict__ psi, i64 count, BitInsert bi,
+__global__ void __launch_bounds__(256) k_swap(typename T::S* __restrict__ psi, i64 count, const __grid_constant__ BitInsert bi,
                                               i64 cmask, i64 sa, i64 sb) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < count; t += stride) {
@@ -444,6 +527,35 @@ int launch_dense(void* state, int n, const GateOp& g, cudaStream_t s) {
       k_1q_pairs<T><<<blocks, 256, 0, s>>>((S*)state, ngroups, b, u00, u01, u10, u11);
       QGB_LAUNCH_CHECK("k_1q_pairs");
       return QGB_OK;
+    }
+  }
+  if constexpr (std::is_same<T, DF128>::value) {
+    // 1-qubit gates with controls and 2-qubit gates: k_dense_mix
+    if (k == 1 || k == 2) {
+      const int nf64 = df_fp64_warps();
+      const int blocks = (int)std::max<i64>(1, std::min<i64>((ngroups + MIX_THREADS - 1) / MIX_THREADS,
+                                                             qgb_num_sms()));
+      const auto launch = [&](auto kk) -> int {
+        constexpr int KK = decltype(kk)::value;
+        Offs<KK> off;
+        CoefDense<KK> cu;
+        for (int m = 0; m < D; ++m) {
+          i64 o = 0;
+          for (int j = 0; j < k; ++j)
+            if ((m >> (k - 1 - j)) & 1) o |= (i64)1 << g.tbits[j];
+          off.o[m] = o;
+          for (int c = 0; c < D; ++c) {
+            cu.d[m][c] = DF128::coef(M[m * D + c].real(), M[m * D + c].imag());
+            cu.e[m][c] = TC128::coef(M[m * D + c].real(), M[m * D + c].imag());
+          }
+        }
+        const int bytes = DENSE_STAGES(KK) * D * MIX_THREADS * (int)sizeof(double2);
+        if (int st = qgb_func_smem((const void*)k_dense_mix<KK>, bytes)) return st;
+        k_dense_mix<KK><<<blocks, MIX_THREADS, bytes, s>>>((double2*)state, ngroups, bi, cmask, off, nf64, cu);
+        QGB_LAUNCH_CHECK("k_dense_mix");
+        return QGB_OK;
+      };
+      return k == 1 ? launch(std::integral_constant<int, 1>()) : launch(std::integral_constant<int, 2>());
     }
   }
   int blocks;
