@@ -94,14 +94,24 @@ __global__ void __launch_bounds__(256) k_collapse_norm(const typename T::S* __re
   collapse_target(a, *outcome, &mask, &value);
   typename T::Acc acc = T::acc_zero();
   const i64 stride = (i64)gridDim.x * blockDim.x;
+  // four kept amplitudes per step: their loads are in flight together
+  constexpr int W = 4;
   int it = 0;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nkept; t += stride, ++it) {
-    i64 idx = t;
-    for (int j = 0; j < a.nq; ++j) {
-      const int p = a.sorted[j];
-      idx = ((idx >> p) << (p + 1)) | (idx & ((((i64)1) << p) - 1));
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < nkept; t += W * stride) {
+    typename T::V v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      i64 idx = t + w * stride;
+      if (idx >= nkept) break;
+      for (int j = 0; j < a.nq; ++j) {
+        const int p = a.sorted[j];
+        idx = ((idx >> p) << (p + 1)) | (idx & ((((i64)1) << p) - 1));
+      }
+      v[w] = T::load(psi, idx | (i64)value);
     }
-    acc = T::acc_add(acc, T::load(psi, idx | (i64)value), it & 1);
+#pragma unroll
+    for (int w = 0; w < W; ++w, ++it)
+      if (t + w * stride < nkept) acc = T::acc_add(acc, v[w], it & 1);
   }
   const double sum = block_sum(T::acc_value(acc));
   if (threadIdx.x == 0) part[blockIdx.x] = sum;
@@ -125,9 +135,19 @@ __global__ void __launch_bounds__(256) k_collapse_apply(typename T::S* __restric
   collapse_target(a, *outcome, &mask, &value);
   const double inv = norm2 ? 1.0 / sqrt(*norm2) : 1.0;
   const i64 stride = (i64)gridDim.x * blockDim.x;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += stride) {
-    const bool keep = ((uint64_t)i & mask) == value;
-    T::store(psi, i, keep ? T::scale(T::load(psi, i), inv) : T::zero());
+  // four amplitudes per step: the loads of the kept ones are in flight
+  // together before any store waits on them
+  constexpr int W = 4;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += W * stride) {
+    typename T::V v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const i64 j = i + w * stride;
+      v[w] = j < N && ((uint64_t)j & mask) == value ? T::scale(T::load(psi, j), inv) : T::zero();
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+      if (i + w * stride < N) T::store(psi, i + w * stride, v[w]);
   }
 }
 

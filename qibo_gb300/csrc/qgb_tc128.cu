@@ -464,12 +464,15 @@ __device__ __forceinline__ void oz_issue(uint32_t s_base, uint32_t tmem, uint32_
 // group CG (reals 16 CG .. 16 CG + 15 of the half, i.e. outputs
 // c = 16 H + 8 CG .. + 7): the seven levels of 8 reals (4 outputs) at a
 // time from TMEM, combined and stored straight to the state; orm collects
-// the OR of the fixed-point outputs' |high words|.
+// the OR of the fixed-point outputs' |high words|.  The loop over the two
+// groups of 8 reals stays rolled: unrolled, the four instances of this
+// function made the kernel's code large enough that its warps stalled on
+// instruction fetch (n=30 chain block 9.2 ms unrolled, 7.3 ms rolled).
 template <bool FIX, int H, int CG>
 __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const OzGeom& geo, const OzGate& G,
                                             const OzShift& fsh, int scale, uint32_t& orm) {
   const uint32_t th = trow + OZ_HALF_COLS * H;
-#pragma unroll
+#pragma unroll 1
   for (int q = 0; q < 2; ++q) {
     const int c4 = 2 * CG + q;
     float acc[OZ_NLEVEL][8];
