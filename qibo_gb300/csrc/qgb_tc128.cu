@@ -69,7 +69,7 @@
 // an in-flight copy, and tensor memory is freed.
 //
 // Runs of unitary blocks (qgb_run_oz_chain) keep the state in a 64-bit
-// fixed-point format between blocks (k_fused5_oz<true>), converted from and
+// fixed-point format between blocks (k_fused5_oz<true, *>), converted from and
 // back to IEEE doubles once per run.
 #include <algorithm>
 #include <cmath>
@@ -138,6 +138,7 @@ struct OzGeom {
   uint32_t aoff_hi[OZ_STEPS];
   i64 rowoff[128];
   i64 coloff[32];
+  int pair;  // outputs 2 m and 2 m + 1 of a row are adjacent amplitudes at an even index
 };
 
 // The (permuted) block in FP64 and, per output row r, the biased exponent of
@@ -460,6 +461,12 @@ __device__ __forceinline__ void oz_issue(uint32_t s_base, uint32_t tmem, uint32_
   }
 }
 
+// two adjacent amplitudes in one 32-byte store (p 32-byte aligned)
+__device__ __forceinline__ void oz_st32(double2* p, double2 a, double2 b) {
+  asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};\n" ::"l"(p), "d"(a.x), "d"(a.y), "d"(b.x), "d"(b.y)
+               : "memory");
+}
+
 // The epilogue's work on output half H of a tile for a warp of column
 // group CG (reals 16 CG .. 16 CG + 15 of the half, i.e. outputs
 // c = 16 H + 8 CG .. + 7): the seven levels of 8 reals (4 outputs) at a
@@ -468,7 +475,7 @@ __device__ __forceinline__ void oz_issue(uint32_t s_base, uint32_t tmem, uint32_
 // groups of 8 reals stays rolled: unrolled, the four instances of this
 // function made the kernel's code large enough that its warps stalled on
 // instruction fetch (n=30 chain block 9.2 ms unrolled, 7.3 ms rolled).
-template <bool FIX, int H, int CG>
+template <bool FIX, bool PAIR, int H, int CG>
 __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const OzGeom& geo, const OzGate& G,
                                             const OzShift& fsh, int scale, uint32_t& orm) {
   const uint32_t th = trow + OZ_HALF_COLS * H;
@@ -480,21 +487,32 @@ __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const O
     for (int l = 0; l < OZ_NLEVEL; ++l) tmem_ld8(th + 32 * l + 8 * c4, acc[l]);
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      const int c = 16 * H + 4 * c4 + (e >> 1);  // output amplitude (permuted block index)
-      float are[OZ_NLEVEL], aim[OZ_NLEVEL];
+    for (int ep = 0; ep < 8; ep += 4) {
+      const int c = 16 * H + 4 * c4 + (ep >> 1);  // outputs c, c + 1 (permuted block index)
+      double2 out[2];
 #pragma unroll
-      for (int l = 0; l < OZ_NLEVEL; ++l) {
-        are[l] = acc[l][e];
-        aim[l] = acc[l][e + 1];
+      for (int h = 0; h < 2; ++h) {
+        const int e = ep + 2 * h;
+        float are[OZ_NLEVEL], aim[OZ_NLEVEL];
+#pragma unroll
+        for (int l = 0; l < OZ_NLEVEL; ++l) {
+          are[l] = acc[l][e];
+          aim[l] = acc[l][e + 1];
+        }
+        if (FIX) {
+          const int64_t xr = oz_combine_fix(are, fsh), xi = oz_combine_fix(aim, fsh);
+          orm |= (uint32_t)abs((int32_t)((uint64_t)xr >> 32)) | (uint32_t)abs((int32_t)((uint64_t)xi >> 32));
+          out[h] = make_double2(oz_bitsd((uint64_t)xr), oz_bitsd((uint64_t)xi));
+        } else {
+          const int sc = scale + G.fexp[c + h] - 2098;
+          out[h] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+        }
       }
-      if (FIX) {
-        const int64_t xr = oz_combine_fix(are, fsh), xi = oz_combine_fix(aim, fsh);
-        orm |= (uint32_t)abs((int32_t)((uint64_t)xr >> 32)) | (uint32_t)abs((int32_t)((uint64_t)xi >> 32));
-        dst[geo.coloff[c]] = make_double2(oz_bitsd((uint64_t)xr), oz_bitsd((uint64_t)xi));
+      if (PAIR) {
+        oz_st32(dst + geo.coloff[c], out[0], out[1]);
       } else {
-        const int sc = scale + G.fexp[c] - 2098;
-        dst[geo.coloff[c]] = make_double2(oz_combine(are, sc), oz_combine(aim, sc));
+        dst[geo.coloff[c]] = out[0];
+        dst[geo.coloff[c + 1]] = out[1];
       }
     }
   }
@@ -502,7 +520,11 @@ __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const O
 
 // FIX: the state holds fixed-point integers (oz_to_fix) instead of IEEE
 // doubles; the launch's scale is then one shift for all tiles, and each
-// output a rounding shift.
+// output a rounding shift.  PAIR (blocks on index bit 0, geo.pair): a lane's
+// outputs c and c + 1 are adjacent amplitudes and go out as one 32-byte
+// store, so a warp's stores stay whole sectors (lanes are 64 bytes or more
+// apart on such blocks); a separate instance, because a runtime choice
+// between the two store forms cost the other placements 2-3 %.
 //
 // Handoffs (each mbarrier phase completes once per tile, or once per two
 // tiles for m_scale[b]; no waiter can fall two phases behind, because every
@@ -510,13 +532,14 @@ __device__ __forceinline__ void oz_epi_half(double2* dst, uint32_t trow, const O
 // consumed upstream):
 //   m_raw    bulk copies -> converters    the raw tile is in shared memory
 //   m_rawfree  converter -> copy warp     the raw tile has been read
-//   m_ready[s]  converter -> MMA          A slice s of tile i written
+//   m_ready[s]  converters -> MMA  (one arrival per converter warp)
+//            A slice s of tile i written
 //   m_free[s]   tcgen05.commit -> converter   the MMAs of tile i that read
 //            slice s are done (the last ones, of half 1)
 //   m_scale[i & 1]  converter -> epilogue  (doubles) scale of tile i in tile_scale[i & 1]
 //   m_full[h]  tcgen05.commit -> epilogue   MMAs of half h of tile i done
 //   m_tfree[h] epilogue (256 arrivals) -> MMA   half h of tile i read
-template <bool FIX>
+template <bool FIX, bool PAIR>
 __global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registers
     k_fused5_oz(double2* __restrict__ psi, i64 ntiles, const __grid_constant__ OzGeom geo,
                 const __grid_constant__ OzGate G, int* __restrict__ err, const uint32_t* __restrict__ fix_in,
@@ -553,7 +576,7 @@ __global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registe
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_raw)));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_rawfree)));
     for (int k = 0; k < OZ_NSLICE; ++k) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_ready[k])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&m_ready[k])), "r"(OZ_CONV_WARPS));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_free[k])));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&m_drain)));
@@ -660,8 +683,10 @@ __global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registe
         } else {
           *abort_v = 1;
         }
-        oz_bar(1);
-        if (g == 0 && !*abort_v) oz_arrive(smem_u32(&m_ready[s]));
+        // one arrival per warp once its lanes have written slice s (a
+        // barrier of all converter threads per slice was 2-5 % slower)
+        __syncwarp();
+        if (lane == 0 && ok) oz_arrive(smem_u32(&m_ready[s]));
       }
       if (!FIX && g == 0 && ok) {
         tile_scale[it & 1] = scale;  // read by the epilogue of tile it - 2 long ago
@@ -718,8 +743,8 @@ __global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registe
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      if (cg == 0) oz_epi_half<FIX, 0, 0>(dst, trow, geo, G, fsh, scale, orm);
-      else oz_epi_half<FIX, 0, 1>(dst, trow, geo, G, fsh, scale, orm);
+      if (cg == 0) oz_epi_half<FIX, PAIR, 0, 0>(dst, trow, geo, G, fsh, scale, orm);
+      else oz_epi_half<FIX, PAIR, 0, 1>(dst, trow, geo, G, fsh, scale, orm);
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       oz_arrive(smem_u32(&m_tfree[0]));  // half 0 read: the next tile's MMAs may write it
       if (!__all_sync(0xffffffffu, oz_wait(smem_u32(&m_full[1]), (uint32_t)it & 1, abort_v))) {
@@ -727,8 +752,8 @@ __global__ void __maxnreg__(96)  // 18 warps: five share one SMSP's 16 K registe
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      if (cg == 0) oz_epi_half<FIX, 1, 0>(dst, trow, geo, G, fsh, scale, orm);
-      else oz_epi_half<FIX, 1, 1>(dst, trow, geo, G, fsh, scale, orm);
+      if (cg == 0) oz_epi_half<FIX, PAIR, 1, 0>(dst, trow, geo, G, fsh, scale, orm);
+      else oz_epi_half<FIX, PAIR, 1, 1>(dst, trow, geo, G, fsh, scale, orm);
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       oz_arrive(smem_u32(&m_tfree[1]));
     }
@@ -853,6 +878,15 @@ void make_oz_geom(int n, const std::vector<int>& tbits, OzGeom* geo, int cbit[5]
   geo->nrest = 0;
   for (int b = 0; b < n; ++b)
     if (std::find(pos.begin(), pos.end(), b) == pos.end()) geo->rest[geo->nrest++] = b;
+  // a block on index bit 0 puts output pairs next to each other: the
+  // epilogue then stores 32 bytes per pair
+  geo->pair = 1;
+  for (int c = 0; c < 32; c += 2)
+    if (geo->coloff[c + 1] != geo->coloff[c] + 1 || (geo->coloff[c] & 1)) geo->pair = 0;
+  for (int r = 0; r < 128; ++r)
+    if (geo->rowoff[r] & 1) geo->pair = 0;
+  for (int j = 0; j < geo->nrest; ++j)
+    if (geo->rest[j] == 0) geo->pair = 0;
 }
 
 // permuted block U'[r'][c'] = U[idx[r']][idx[c']] (see make_oz_geom) and the
@@ -907,8 +941,12 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
   OzGate* G = new OzGate();
   int cbit[5];
   make_oz_geom(n, g.tbits, geo, cbit);
+  if ((uintptr_t)state % 32 != 0) geo->pair = 0;  // 32-byte stores need a 32-byte aligned state
   make_oz_gate(g, cbit, G, fix);
-  const int sa = qgb_func_smem(fix ? (const void*)k_fused5_oz<true> : (const void*)k_fused5_oz<false>, OZ_SMEM);
+  const bool pair = geo->pair != 0;
+  const void* kfn = fix ? (pair ? (const void*)k_fused5_oz<true, true> : (const void*)k_fused5_oz<true, false>)
+                        : (pair ? (const void*)k_fused5_oz<false, true> : (const void*)k_fused5_oz<false, false>);
+  const int sa = qgb_func_smem(kfn, OZ_SMEM);
   if (sa) {
     delete G;
     delete geo;
@@ -916,12 +954,17 @@ int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bo
   }
   const i64 ntiles = (i64)1 << (n - 12);
   const int blocks = (int)std::min<i64>(ntiles, (i64)qgb_num_sms());
-  if (fix)
-    k_fused5_oz<true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, fix_words + b % 3,
-                                                          fix_words + (b + 1) % 3, fix_words + (b + 2) % 3);
+  uint32_t* const f0 = fix ? fix_words + b % 3 : nullptr;
+  uint32_t* const f1 = fix ? fix_words + (b + 1) % 3 : nullptr;
+  uint32_t* const f2 = fix ? fix_words + (b + 2) % 3 : nullptr;
+  if (fix && pair)
+    k_fused5_oz<true, true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, f0, f1, f2);
+  else if (fix)
+    k_fused5_oz<true, false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, f0, f1, f2);
+  else if (pair)
+    k_fused5_oz<false, true><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, f0, f1, f2);
   else
-    k_fused5_oz<false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, nullptr, nullptr,
-                                                           nullptr);
+    k_fused5_oz<false, false><<<blocks, OZ_THREADS, OZ_SMEM, s>>>((double2*)state, ntiles, *geo, *G, err, f0, f1, f2);
   delete G;
   delete geo;
   QGB_LAUNCH_CHECK("k_fused5_oz");

@@ -238,6 +238,8 @@ int main() {
       int cbit[5];
       make_oz_geom(n, tb, geo, cbit);
       make_oz_gate(g, cbit, G, false);
+      // paired stores exactly when index bit 0 is a block qubit
+      if (geo->pair != (int)(std::find(tb.begin(), tb.end(), 0) != tb.end())) fails++;
       int t5 = 0;
       for (int b : tb) t5 += b < 5;
       const i64 N = (i64)1 << n;
@@ -345,9 +347,12 @@ int main() {
               }
               vals[part] = oz_combine(acc, exm + G->fexp[c] - 2098);
             }
-            // the epilogue's direct store of (row, c)
+            // the epilogue's direct store of (row, c); with geo->pair, outputs
+            // c and c + 1 (c even) go out as one 32-byte store at gi
             const i64 gi = base + geo->rowoff[row] + geo->coloff[c];
             if (gi < 0 || gi >= N) { bad = true; continue; }
+            if (geo->pair && (c & 1) == 0 && ((gi & 1) || base + geo->rowoff[row] + geo->coloff[c + 1] != gi + 1))
+              bad = true;
             wrote[gi]++;
             out[gi] = cd(vals[0], vals[1]);
             bound[gi] = std::ldexp(1.0, (exm - 1022) + (G->fexp[c] - 1022) - 41);
