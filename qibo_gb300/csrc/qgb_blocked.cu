@@ -163,9 +163,11 @@ __device__ __forceinline__ void pass_body(typename T::G* __restrict__ psi, i64 n
 }
 
 // Passes whose dense blocks have at most 2 qubits (the common case) are
-// compiled for two resident CTAs per SM; passes with 3-5-qubit fused blocks
-// get the full register file.
-#define QGB_PASS_MIN_CTAS(MAXK) ((MAXK) <= 2 ? 2 : 1)
+// compiled for three resident CTAs per SM (at most 85 registers a thread:
+// the complex128 pass then fits three 64 KB tiles per SM instead of two,
+// QFT(30) 283 -> 260 ms, a depth-10 brickwork 1576 -> 1341 ms); passes with
+// 3-5-qubit fused blocks get the full register file.
+#define QGB_PASS_MIN_CTAS(MAXK) ((MAXK) <= 2 ? 3 : 1)
 
 template <typename T, int MAXK>
 __global__ void __launch_bounds__(256, QGB_PASS_MIN_CTAS(MAXK))
