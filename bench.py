@@ -1145,6 +1145,45 @@ def run_memlimit(args):
     print(json.dumps({"workload": "memory limit: QFT + depth-10 brickwork, 1e7 shots, <ZZ>", **res}))
 
 
+def run_chain(args):
+    """The complex128 block kernel in a fixed-point chain at ``--nqubits``:
+    a random 5-qubit unitary on three placements (qubits 0..4 = the top
+    index bits, the middle five, and qubits n-5..n-1 = index bits 0..4), on
+    a state first made dense; ms per block = (chain of 10 - chain of 2) / 8,
+    CUDA events on the launch stream, so the chain's norm and conversion
+    passes cancel.  2 * 2^n * 16 bytes per block."""
+    from qibo_gb300._lib import check
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+
+    n = args.nqubits
+    b = GB300Backend("complex128")
+    rt, eng, lib = b.rt, b.engine_gb, b.rt.lib
+    st = DeviceState(n, "complex128")
+    rng = np.random.default_rng(1)
+    q, r = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))
+    u = q * (np.diag(r) / np.abs(np.diag(r)))
+    check(lib.qgb_state_zero(st.ptr, n, st.code, rt.stream))
+    eng.apply_many(st, [(list(range(5 * k, 5 * k + 5)), [], u) for k in range(n // 5)], blocked=True)
+    ev = Events(lib)
+    peak = measured_peaks().get("hbm_gbs", 6800.0)
+
+    def timed(descs):
+        eng.apply_many(st, descs, blocked=True)
+        ev.start(rt.stream)
+        eng.apply_many(st, descs, blocked=True)
+        return ev.stop_ms(rt.stream)
+
+    rows = {}
+    for name, qs in (("top index bits", [0, 1, 2, 3, 4]), ("middle", list(range(n // 2 - 2, n // 2 + 3))),
+                     ("index bits 0..4", [n - 5, n - 4, n - 3, n - 2, n - 1])):
+        ms = (timed([(qs, [], u)] * 10) - timed([(qs, [], u)] * 2)) / 8
+        gbs = 2 * 2**n * 16 / (ms * 1e-3) / 1e9
+        rows[name] = {"ms_per_block": round(ms, 3), "GB/s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3)}
+    print(json.dumps({"workload": f"complex128 block kernel in a fixed-point chain, n={n}", "hbm_peak_gbs": peak,
+                      **rows}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1152,7 +1191,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="brickwork",
-                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels", "fusion"])
+                    choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels", "fusion",
+                             "chain"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
@@ -1167,7 +1207,7 @@ def main():
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
             "memlimit": run_memlimit, "tc5": run_tc5, "kernels": run_kernels,
-            "fusion": run_fusion}[args.workload](args)
+            "fusion": run_fusion, "chain": run_chain}[args.workload](args)
 
 
 if __name__ == "__main__":
