@@ -1145,6 +1145,49 @@ def run_memlimit(args):
     print(json.dumps({"workload": "memory limit: QFT + depth-10 brickwork, 1e7 shots, <ZZ>", **res}))
 
 
+def run_density(args):
+    """A noisy circuit on a density matrix of ``--nqubits`` qubits (at most
+    16; 14 by default, a 28-qubit vector of 4.3 GB in complex128): depth 10
+    of U3 on every qubit, CZ on brickwork pairs, then a depolarizing channel
+    (p = 0.01) and amplitude damping (gamma = 0.05) on every qubit.  Timed
+    through the public API (``execute_circuit`` on a density-matrix circuit,
+    the device synchronised), median of ``--steps`` runs after ``--warmup``.
+    Reports the trace and the purity Tr(rho^2) (the squared norm of the
+    entry vector) of the result."""
+    from qibo_gb300 import Circuit, gates as G
+    from qibo_gb300.backend import GB300Backend
+
+    n = args.nqubits if args.nqubits <= 16 else 14
+    backend = GB300Backend(args.dtype)
+    rng = np.random.default_rng(14)
+    c = Circuit(n, density_matrix=True)
+    depth = 10
+    for layer in range(depth):
+        for q in range(n):
+            c.add(G.U3(q, *rng.uniform(0, 2 * np.pi, 3)))
+        for q in range(layer % 2, n - 1, 2):
+            c.add(G.CZ(q, q + 1))
+        for q in range(n):
+            c.add(G.DepolarizingChannel((q,), 0.01))
+            c.add(G.AmplitudeDampingChannel(q, 0.05))
+    times = []
+    res = None
+    for i in range(args.warmup + args.steps):
+        backend.rt.synchronize()
+        t0 = time.perf_counter()
+        res = backend.execute_circuit(c)
+        backend.rt.synchronize()
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    rho = res.state()
+    sec = statistics.median(times)
+    print(json.dumps({"workload": f"noisy density matrix, n={n} ({2 * n}-qubit vector), depth {depth}",
+                      "dtype": args.dtype, "gates": n * depth + sum(len(range(l % 2, n - 1, 2)) for l in range(depth)),
+                      "channels": 2 * n * depth, "seconds": sec,
+                      "vector_gb": 4**n * (16 if args.dtype == "complex128" else 8) / 1e9,
+                      "trace": backend.engine_gb.density_trace(rho), "purity": backend.engine_gb.norm2(rho)}))
+
+
 def run_chain(args):
     """The complex128 block kernel in a fixed-point chain at ``--nqubits``:
     a random 5-qubit unitary on three placements (qubits 0..4 = the top
@@ -1192,7 +1235,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="brickwork",
                     choices=["brickwork", "qft20", "vqe24", "serving", "memlimit", "tc5", "kernels", "fusion",
-                             "chain"])
+                             "chain", "density"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
     ap.add_argument("--dtype", default="complex128")
     ap.add_argument("--mode", default="auto", choices=["auto", "gates", "blocked", "fused", "engine"])
@@ -1207,7 +1250,7 @@ def main():
         return run_reference(args)
     return {"brickwork": run_brickwork, "qft20": run_qft20, "vqe24": run_vqe24, "serving": run_serving,
             "memlimit": run_memlimit, "tc5": run_tc5, "kernels": run_kernels,
-            "fusion": run_fusion, "chain": run_chain}[args.workload](args)
+            "fusion": run_fusion, "chain": run_chain, "density": run_density}[args.workload](args)
 
 
 if __name__ == "__main__":
