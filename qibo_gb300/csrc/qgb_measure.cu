@@ -571,8 +571,9 @@ struct TermSet {
   u64 zmask[QGB_TERMS_PER_LAUNCH];   // amplitude-index bit masks
   double coef[QGB_TERMS_PER_LAUNCH]; // diagonal: c_t; flip: c_t f_t (see k_expect_flip)
   float chi[QGB_TERMS_PER_LAUNCH], clo[QGB_TERMS_PER_LAUNCH];  // coef as a double-float
-  // diagonal terms on 2^10 amplitudes or more: terms sorted by m = index
-  // bits 5..9 of their mask, [mstart[m], mstart[m+1]) having that m
+  // diagonal terms on 2^(5 + WB) amplitudes or more (k_expect_diag_wht):
+  // terms sorted by m = index bits 5..4+WB of their mask, [mstart[m],
+  // mstart[m+1]) having that m
   uint32_t mused;
   int mstart[33];
   // flip terms: bit k set when term k uses Im(conj(psi_i) psi_j), else Re
@@ -581,7 +582,7 @@ struct TermSet {
 };
 
 // Terms with no X/Y factor: sum_i |psi_i|^2 * sum_t c_t (-1)^popc(i & z_t)
-// (states of fewer than 2^10 amplitudes).
+// (states of fewer than 2^(5 + WB) amplitudes, WB of k_expect_diag_wht).
 template <typename T>
 __global__ void __launch_bounds__(256) k_expect_diag(const typename T::S* __restrict__ psi, i64 N,
                                                      const __grid_constant__ TermSet ts, double* __restrict__ part) {
@@ -635,11 +636,23 @@ __global__ void __launch_bounds__(256) k_expect_diag_wht(const typename T::S* __
 #pragma unroll
     for (int m = 0; m < K; ++m) {
       if (!((ts.mused >> m) & 1)) continue;
-      DFAcc cm{0.f, 0.f};
-      for (int t = ts.mstart[m]; t < ts.mstart[m + 1]; ++t) {
-        const bool odd = __popcll((u64)base & ts.zmask[t]) & 1;
-        cm = df_plus(cm, odd ? DFAcc{-ts.chi[t], -ts.clo[t]} : DFAcc{ts.chi[t], ts.clo[t]});
+      // the run's signed coefficient sum, in four independent partial sums
+      // (a single chain of double-float additions was latency-bound)
+      DFAcc c4[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      const int te = ts.mstart[m + 1];
+      int t = ts.mstart[m];
+      for (; t + 4 <= te; t += 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const bool odd = __popcll((u64)base & ts.zmask[t + j]) & 1;
+          c4[j] = df_plus(c4[j], odd ? DFAcc{-ts.chi[t + j], -ts.clo[t + j]} : DFAcc{ts.chi[t + j], ts.clo[t + j]});
+        }
       }
+      for (; t < te; ++t) {
+        const bool odd = __popcll((u64)base & ts.zmask[t]) & 1;
+        c4[0] = df_plus(c4[0], odd ? DFAcc{-ts.chi[t], -ts.clo[t]} : DFAcc{ts.chi[t], ts.clo[t]});
+      }
+      const DFAcc cm = df_plus(df_plus(c4[0], c4[1]), df_plus(c4[2], c4[3]));
       // acc += cm * S[m]: the product of the heads split exactly, the cross terms added
       const float ph = cm.hi * p[m].hi;
       acc = df_add2(acc, ph, fmaf(cm.hi, p[m].hi, -ph) + fmaf(cm.hi, p[m].lo, cm.lo * p[m].hi));
