@@ -585,10 +585,20 @@ class GB300Methods:
         return out
 
     def sample_frequencies(self, probabilities, nshots):
+        """Counter of outcome -> count.  The shots are the same draws either
+        way: with fewer shots than outcomes they are copied back and counted
+        on the host (nshots int64 instead of a 2^m histogram), otherwise the
+        histogram is built on the device; the Counter is filled from whole
+        arrays."""
         n = len(probabilities)
-        counts = self.engine_gb.sample(self._device_probs(probabilities), int(nshots), self._next_key(), counts=True)
-        nz = np.nonzero(counts[:n])[0]
-        return collections.Counter({int(i): int(counts[i]) for i in nz})
+        probs = self._device_probs(probabilities)
+        if int(nshots) < n:
+            shots = self.engine_gb.sample(probs, int(nshots), self._next_key(), counts=False)
+            vals, cnts = np.unique(shots, return_counts=True)
+            return collections.Counter(dict(zip(vals.tolist(), cnts.tolist())))
+        counts = self.engine_gb.sample(probs, int(nshots), self._next_key(), counts=True)
+        nz = np.flatnonzero(counts[:n])
+        return collections.Counter(dict(zip(nz.tolist(), counts[nz].tolist())))
 
     # -- observables ----------------------------------------------------------
     def expectation_value(self, hamiltonian, state, normalize):
