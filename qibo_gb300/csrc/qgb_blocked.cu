@@ -167,6 +167,11 @@ __device__ __forceinline__ void pass_body(typename T::G* __restrict__ psi, i64 n
 // the complex128 pass then fits three 64 KB tiles per SM instead of two,
 // QFT(30) 283 -> 260 ms, a depth-10 brickwork 1576 -> 1341 ms); passes with
 // 3-5-qubit fused blocks get the full register file.
+// most norm-growth bits of one fixed-point chain of complex128 blocks (each
+// bit of headroom is one bit less between the state's norm and 2^61 at the
+// chain's start; the 47-bit digit windows follow the values, not the norm)
+#define QGB_OZ_HEADROOM 8
+
 #define QGB_PASS_MIN_CTAS(MAXK) ((MAXK) <= 2 ? 3 : 1)
 
 template <typename T, int MAXK>
@@ -429,23 +434,45 @@ int qgb_run_blocked(void* state, int nqubits, int dtype, const qgb_op* ops, int 
   }
   const bool tc_ok = use_tc && (dtype == QGB_C64 || (dtype == QGB_C128 && nqubits >= 12 && !strict_fp64));
   if (!tc_ok) return run_segment(state, nqubits, dtype, g, strict_fp64, s);
-  // consecutive tensor-core blocks; a complex128 run of two or more unitary
-  // blocks runs as one fixed-point chain
+  // consecutive tensor-core blocks; in complex128, runs of two or more
+  // blocks whose norm growth (qgb_oz_growth_bits: 0 for unitary blocks,
+  // e.g. density-matrix channels otherwise) adds up to at most
+  // QGB_OZ_HEADROOM bits run as fixed-point chains with that headroom; a
+  // block left alone runs on IEEE doubles
   std::vector<const GateOp*> run;
   auto flush_run = [&]() -> int {
     if (run.empty()) return QGB_OK;
     int st = QGB_OK;
-    bool chain = dtype == QGB_C128 && run.size() >= 2;
-    for (const GateOp* b : run) chain = chain && qgb_oz_unitary(*b);
-    if (chain) {
-      st = qgb_run_oz_chain(state, nqubits, run, s);
-    } else {
+    if (dtype != QGB_C128) {
       for (const GateOp* b : run) {
-        st = dtype == QGB_C128 ? qgb_launch_fused5_oz(state, nqubits, *b, s, false)
-                               : qgb_launch_fused5_tc(state, nqubits, *b, s);
+        st = qgb_launch_fused5_tc(state, nqubits, *b, s);
         if (st) break;
       }
+      run.clear();
+      return st;
     }
+    std::vector<const GateOp*> chain;
+    int head = 0;
+    auto flush_chain = [&]() -> int {
+      int r = QGB_OK;
+      if (chain.size() >= 2) r = qgb_run_oz_chain(state, nqubits, chain, s, head);
+      else if (chain.size() == 1) r = qgb_launch_fused5_oz(state, nqubits, *chain[0], s, false);
+      chain.clear();
+      head = 0;
+      return r;
+    };
+    for (const GateOp* b : run) {
+      const int gb = qgb_oz_growth_bits(*b);
+      if (gb > QGB_OZ_HEADROOM) {  // too expansive for any chain: alone, on IEEE doubles
+        if ((st = flush_chain())) break;
+        if ((st = qgb_launch_fused5_oz(state, nqubits, *b, s, false))) break;
+        continue;
+      }
+      if (head + gb > QGB_OZ_HEADROOM && (st = flush_chain())) break;
+      chain.push_back(b);
+      head += gb;
+    }
+    if (!st) st = flush_chain();
     run.clear();
     return st;
   };

@@ -38,7 +38,8 @@ int qgb_launch_fused5_tc(void* state, int n, const GateOp& g, cudaStream_t s);
 int qgb_launch_fused5_oz(void* state, int n, const GateOp& g, cudaStream_t s, bool fix,
                          uint32_t* fix_words = nullptr, int b = 0);
 bool qgb_oz_unitary(const GateOp& g);
-int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s);
+int qgb_oz_growth_bits(const GateOp& g);
+int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s, int headroom);
 int qgb_tc_prepare();  // allocate the tensor-core paths' device buffers (idempotent)
 int qgb_oz_stream_prepare(cudaStream_t s);  // complex128 chain scratch of stream s (qgb_tc128.cu)
 int qgb_oz_stream_release(cudaStream_t s);  // and its release before the stream is destroyed

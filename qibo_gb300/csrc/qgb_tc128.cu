@@ -68,7 +68,8 @@
 // then waits once more (bounded) for its in-flight MMAs, the copy warp for
 // an in-flight copy, and tensor memory is freed.
 //
-// Runs of unitary blocks (qgb_run_oz_chain) keep the state in a 64-bit
+// Runs of blocks (qgb_run_oz_chain; non-unitary ones with headroom for
+// their norm growth, qgb_oz_growth_bits) keep the state in a 64-bit
 // fixed-point format between blocks (k_fused5_oz<true, *>), converted from and
 // back to IEEE doubles once per run.
 #include <algorithm>
@@ -359,7 +360,8 @@ __host__ __device__ __forceinline__ int64_t oz_combine_fix(const float acc[OZ_NL
 
 // Fixed-point state format between consecutive tensor-core blocks: a real
 // x is held as the integer X = round(x 2^(62 - e)), e a state-wide scale with
-// 2^e > 2 ||psi|| (so |X| < 2^61, and unitary blocks keep it there).
+// 2^e > 2 ||psi|| (so |X| < 2^61, and unitary blocks keep it there; a chain
+// of blocks that can grow the norm by g bits in all starts g bits higher).
 __host__ __device__ __forceinline__ int64_t oz_to_fix(double x, int e) {
   const uint64_t u = oz_dbits(x);
   const uint32_t hi = (uint32_t)(u >> 32);
@@ -980,9 +982,11 @@ __host__ __device__ __forceinline__ int oz_scale_exp(double norm2) {
   return norm2 > 0 ? ((x + 1) >> 1) + 1 : 0;
 }
 
-// the scale e, and the chain's first two shift words cleared
-__global__ void k_oz_scale(const double* __restrict__ norm2, int* __restrict__ e, uint32_t* __restrict__ fixw) {
-  *e = oz_scale_exp(*norm2);
+// the scale e (plus the chain's headroom bits: the blocks may grow the
+// norm by that many), and the chain's first two shift words cleared
+__global__ void k_oz_scale(const double* __restrict__ norm2, int* __restrict__ e, uint32_t* __restrict__ fixw,
+                           int headroom) {
+  *e = oz_scale_exp(*norm2) + headroom;
   fixw[0] = 0;
   fixw[1] = 0;
 }
@@ -1021,6 +1025,42 @@ bool qgb_oz_unitary(const GateOp& g) {
       if (std::abs(acc - zd(i == j ? 1.0 : 0.0, 0.0)) > 1e-9) return false;
     }
   return true;
+}
+
+// Bits by which a block can grow the 2-norm of a state: 0 for a unitary
+// block, else ceil(log2 s) for a rigorous bound s on its largest singular
+// value: s^2 = lambda_max(M), M = B^H B, is at most ||M^8||_inf^(1/8)
+// (the largest absolute row sum of a matrix power bounds its spectral
+// radius), tight for near-unitary and contractive blocks.
+int qgb_oz_growth_bits(const GateOp& g) {
+  if (qgb_oz_unitary(g)) return 0;
+  std::vector<zd> M(1024, zd(0, 0)), T(1024);
+  for (int i = 0; i < 32; ++i)
+    for (int j = 0; j < 32; ++j) {
+      zd acc = 0;
+      for (int k = 0; k < 32; ++k) acc += std::conj(g.coef[k * 32 + i]) * g.coef[k * 32 + j];
+      M[i * 32 + j] = acc;
+    }
+  for (int sq = 0; sq < 3; ++sq) {  // M <- M^2, three times: M^8
+    for (int i = 0; i < 32; ++i)
+      for (int j = 0; j < 32; ++j) {
+        zd acc = 0;
+        for (int k = 0; k < 32; ++k) acc += M[i * 32 + k] * M[k * 32 + j];
+        T[i * 32 + j] = acc;
+      }
+    M.swap(T);
+  }
+  double row = 0;
+  for (int i = 0; i < 32; ++i) {
+    double r = 0;
+    for (int j = 0; j < 32; ++j) r += std::abs(M[i * 32 + j]);
+    row = std::max(row, r);
+  }
+  if (!(row > 0)) return 0;              // the zero block
+  if (!std::isfinite(row)) return 1 << 20;  // too large to bound: never chained
+  // s = row^(1/16); bits = ceil(log2 s), with a margin for the rounding of the bound
+  const double bits = std::log2(row) / 16.0 + 1e-9;
+  return bits <= 0 ? 0 : (int)std::ceil(bits);
 }
 
 extern "C" int qgb_norm2(const void* state, int nqubits, int dtype, double* out, void* scratch, void* stream);
@@ -1111,17 +1151,19 @@ int qgb_oz_stream_release(cudaStream_t s) {
   return QGB_OK;
 }
 
-// Consecutive unitary blocks on a complex128 state (n >= 12): the state is
+// Consecutive blocks on a complex128 state (n >= 12): the state is
 // converted once to the fixed-point format (scale from its FP64 norm, all on
 // the device), every block runs on it, and it is converted back.  Two extra
 // state passes replace the double <-> digit conversions of every block.
-int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s) {
+// ``headroom``: the blocks' growth bits together (qgb_oz_growth_bits; 0 for
+// unitary blocks), added to the scale so that |X| < 2^61 holds throughout.
+int qgb_run_oz_chain(void* state, int n, const std::vector<const GateOp*>& blocks, cudaStream_t s, int headroom) {
   OzChainScratch* cs;
   int st = qgb_oz_stream_scratch(s, &cs);
   if (st) return st;
   st = qgb_norm2(state, n, QGB_C128, cs->norm, cs->red, (void*)s);
   if (st) return st;
-  k_oz_scale<<<1, 1, 0, s>>>(cs->norm, cs->e, cs->fixw);
+  k_oz_scale<<<1, 1, 0, s>>>(cs->norm, cs->e, cs->fixw, headroom);
   QGB_LAUNCH_CHECK("k_oz_scale");
   const i64 N = (i64)1 << n;
   const int grid = (int)std::min<i64>((N + 255) / 256, (i64)qgb_num_sms() * 8);

@@ -139,10 +139,15 @@ static void replay_fix_block(std::vector<int64_t>& X, int n, const GateOp& g, in
 // from the FP64 norm, oz_to_fix / oz_from_fix at the ends) against the FP64
 // product: 1e-13 absolute on normalised states, including one whose
 // amplitudes span 2^-30..1.  Returns the number of failures.
+// Trials 4-7 scale the columns of each unitary by factors in [0.5, 1.5]:
+// non-unitary blocks (the density-matrix channels' case), chained with the
+// headroom of their growth bits (qgb_oz_growth_bits) added to the scale.
 static int chain_check(std::mt19937_64& rng, int* exact_fails) {
   std::normal_distribution<double> nd;
+  std::uniform_real_distribution<double> ud(0.5, 1.5);
   int fails = 0;
-  for (int trial = 0; trial < 4; ++trial) {
+  for (int trial = 0; trial < 8; ++trial) {
+    const bool grow = trial >= 4;
     const int n = 13 + (trial & 1);
     const i64 N = (i64)1 << n;
     std::vector<cd> psi(N);
@@ -155,13 +160,10 @@ static int chain_check(std::mt19937_64& rng, int* exact_fails) {
     for (auto& x : psi) x /= std::sqrt(nrm2);
     nrm2 = 0;
     for (auto& x : psi) nrm2 += std::norm(x);
-    const int e = oz_scale_exp(nrm2);
-    std::vector<int64_t> X(2 * N);
-    for (i64 i = 0; i < N; ++i) {
-      X[2 * i] = oz_to_fix(psi[i].real(), e);
-      X[2 * i + 1] = oz_to_fix(psi[i].imag(), e);
-    }
-    std::vector<cd> ref = psi;
+    // the three blocks first (their growth sets the chain's headroom)
+    std::vector<GateOp> gs(3);
+    std::vector<std::vector<cd>> Us(3);
+    int head = 0;
     for (int b = 0; b < 3; ++b) {
       std::vector<int> all(n);
       for (int i = 0; i < n; ++i) all[i] = i;
@@ -182,9 +184,30 @@ static int chain_check(std::mt19937_64& rng, int* exact_fails) {
         for (int i = 0; i < 32; ++i) nn += std::norm(U[i * 32 + j]);
         for (int i = 0; i < 32; ++i) U[i * 32 + j] /= std::sqrt(nn);
       }
+      if (grow)
+        for (int j = 0; j < 32; ++j) {
+          const double f = ud(rng);
+          for (int i = 0; i < 32; ++i) U[i * 32 + j] *= f;
+        }
       g.coef.resize(1024);
       for (int i = 0; i < 1024; ++i) g.coef[i] = zd(U[i].real(), U[i].imag());
-      if (!qgb_oz_unitary(g)) fails++;
+      if (qgb_oz_unitary(g) == grow) fails++;
+      const int gb = qgb_oz_growth_bits(g);
+      if (grow ? gb != 1 : gb != 0) fails++;  // singular values in [0.5, 1.5]: one bit
+      head += gb;
+      gs[b] = g;
+      Us[b] = U;
+    }
+    const int e = oz_scale_exp(nrm2) + head;
+    std::vector<int64_t> X(2 * N);
+    for (i64 i = 0; i < N; ++i) {
+      X[2 * i] = oz_to_fix(psi[i].real(), e);
+      X[2 * i + 1] = oz_to_fix(psi[i].imag(), e);
+    }
+    std::vector<cd> ref = psi;
+    for (int b = 0; b < 3; ++b) {
+      const GateOp& g = gs[b];
+      const std::vector<cd>& U = Us[b];
       replay_fix_block(X, n, g, exact_fails);
       std::vector<cd> out(N);
       for (i64 i = 0; i < N; ++i) {
@@ -205,11 +228,15 @@ static int chain_check(std::mt19937_64& rng, int* exact_fails) {
       }
       ref = out;
     }
-    double err = 0;
-    for (i64 i = 0; i < N; ++i)
+    double err = 0, big = 0;
+    for (i64 i = 0; i < N; ++i) {
       err = std::max(err, std::abs(cd(oz_from_fix(X[2 * i], e), oz_from_fix(X[2 * i + 1], e)) - ref[i]));
-    printf("fixed-point chain n=%d trial %d: max abs error %.3g\n", n, trial, err);
-    if (err > 1e-13) fails++;
+      big = std::max(big, std::abs(ref[i]));
+      // the fixed-point range holds: |X| < 2^61 after every block
+      if (std::llabs(X[2 * i]) >= (1ll << 61) || std::llabs(X[2 * i + 1]) >= (1ll << 61)) (*exact_fails)++;
+    }
+    printf("fixed-point chain n=%d trial %d (headroom %d): max abs error %.3g\n", n, trial, head, err);
+    if (err > 1e-13 * std::max(1.0, std::ldexp(1.0, head))) fails++;
   }
   return fails;
 }
