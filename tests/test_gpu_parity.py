@@ -2,7 +2,7 @@
 vectors and the CPU oracle.
 
 Tolerances: complex128 results match the reference to 1e-12 max-abs (the
-spec bar; observed errors are ~1e-15); complex64 results to 1e-5
+drop-in bar for complex128; observed errors are ~1e-15); complex64 results to 1e-5
 max-abs against the complex64 reference run; FP64 probabilities to 1e-14;
 sampled histograms pass a chi-square test at p > 1e-4.
 """
