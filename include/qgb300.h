@@ -43,7 +43,7 @@ extern "C" {
 #define QGB_ERR_OOM 2         /* device allocation failed (backends/abstract.py:2500-2510) */
 #define QGB_ERR_CUDA 3        /* any other CUDA runtime error */
 #define QGB_ERR_TIMEOUT 4     /* a bounded device wait gave up */
-#define QGB_ERR_UNSUPPORTED 5 /* valid request this build does not handle */
+#define QGB_ERR_UNSUPPORTED 5 /* valid request the library does not handle */
 
 #define QGB_C64 0
 #define QGB_C128 1
