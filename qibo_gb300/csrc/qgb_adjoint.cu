@@ -13,9 +13,13 @@
 // derivative inner products per CTA; partial sums are reduced in a fixed
 // order, so results are deterministic.
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <vector>
 
+#include <type_traits>
+
+#include "qgb_df64.cuh"
 #include "qgb_plan.h"
 
 int qgb_launch_gateop(void* state, int n, int dtype, const GateOp& g, cudaStream_t s);  // qgb_gates.cu
@@ -192,6 +196,67 @@ __global__ void __launch_bounds__(256) k_adjoint_step(typename T::S* __restrict_
   }
 }
 
+// Complex128 parametrised 1-qubit gates: the step's three complex 2x2
+// products per amplitude pair (U^dagger psi, the derivatives, U^dagger
+// lambda) bound an IEEE FP64 form by GB300's FP64 pipe, so the pairs are
+// shared as in k_1q_pairs_mix: warps 0-3 (one per scheduler) of every other
+// block compute in IEEE FP64, the others in double-float (error-free row
+// products, the derivative inner products accumulated in double-float and
+// flushed to FP64 per thread).  Which thread handles which pair, and the
+// order of the partial sums, do not depend on the split.
+template <typename T>
+__device__ __forceinline__ void adj_pairs(typename T::S* __restrict__ psi, typename T::S* __restrict__ lam,
+                                          i64 ngroups, const BitInsert& bi, i64 cmask, const Offs5& off, int nder,
+                                          const AdjMats<T, 1>& M, double acc_out[3]) {
+  constexpr bool kDF = std::is_same<T, DF128>::value;
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  double acc[3] = {0.0, 0.0, 0.0};
+  DFAcc dacc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < ngroups; t += stride) {
+    const i64 base = insert_zeros(t, bi) | cmask;
+    const typename T::V v0 = T::load(psi, base + off.o[0]), v1 = T::load(psi, base + off.o[1]);
+    const typename T::V w0 = T::load(lam, base + off.o[0]), w1 = T::load(lam, base + off.o[1]);
+    const typename T::V p0 = T::row2(M.udag[0][0], v0, M.udag[0][1], v1);
+    const typename T::V p1 = T::row2(M.udag[1][0], v0, M.udag[1][1], v1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {  // unrolled: the accumulators stay in registers
+      if (d >= nder) break;
+      const typename T::V m0 = T::row2(M.der[d][0][0], p0, M.der[d][0][1], p1);
+      const typename T::V m1 = T::row2(M.der[d][1][0], p0, M.der[d][1][1], p1);
+      if constexpr (kDF) {  // Re(conj(w0) m0) + Re(conj(w1) m1), one error-free dot product
+        const df x[4] = {w0.re, w0.im, w1.re, w1.im}, y[4] = {m0.re, m0.im, m1.re, m1.im};
+        const float sx[4] = {1.f, 1.f, 1.f, 1.f};
+        const df r = df_dot<4>(x, y, sx);
+        dacc[d] = df_add2(dacc[d], r.hi, r.lo);
+      } else {
+        acc[d] += T::re(w0) * T::re(m0) + T::im(w0) * T::im(m0) + T::re(w1) * T::re(m1) + T::im(w1) * T::im(m1);
+      }
+    }
+    T::store(lam, base + off.o[0], T::row2(M.udag[0][0], w0, M.udag[0][1], w1));
+    T::store(lam, base + off.o[1], T::row2(M.udag[1][0], w0, M.udag[1][1], w1));
+    T::store(psi, base + off.o[0], p0);
+    T::store(psi, base + off.o[1], p1);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) acc_out[d] = kDF ? f2d_exact(dacc[d].hi) + f2d_exact(dacc[d].lo) : acc[d];
+}
+
+__global__ void __launch_bounds__(256) k_adjoint_step_mix(double2* __restrict__ psi, double2* __restrict__ lam,
+                                                          i64 ngroups, const __grid_constant__ BitInsert bi,
+                                                          i64 cmask, Offs5 off, int nder,
+                                                          const __grid_constant__ AdjMats<TC128, 1> Me,
+                                                          const __grid_constant__ AdjMats<DF128, 1> Md,
+                                                          double* __restrict__ part, int part_stride) {
+  __shared__ double sh[8];
+  double acc[3];
+  if ((threadIdx.x >> 7) == 0 && (blockIdx.x & 1) == 0) adj_pairs<TC128>(psi, lam, ngroups, bi, cmask, off, nder, Me, acc);
+  else adj_pairs<DF128>(psi, lam, ngroups, bi, cmask, off, nder, Md, acc);
+  for (int d = 0; d < nder; ++d) {
+    const double s = block_sum_d(acc[d], sh);
+    if (threadIdx.x == 0) part[(i64)blockIdx.x * part_stride + d] = s;
+  }
+}
+
 namespace {
 const int kAdjBlocks = 4 * 152;
 
@@ -238,6 +303,25 @@ int adjoint_step(void* psi, void* lam, int n, const GateOp& g, int nder, const d
   grid_for(ngroups, 256, &blocks);
   blocks = std::min(blocks, kAdjBlocks);
   typedef typename T::S S;
+  if constexpr (std::is_same<T, TC128>::value && K == 1) {
+    const char* strict = getenv("QIBO_GB300_STRICT_FP64");
+    if (!(strict && strict[0] == '1' && strict[1] == 0)) {  // the FP64 / double-float warp split
+      AdjMats<DF128, 1>* Md = new AdjMats<DF128, 1>();
+      for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 2; ++c) {
+          Md->udag[r][c] = DF128::coef(g.coef[r * 2 + c].real(), g.coef[r * 2 + c].imag());
+          for (int d = 0; d < 3; ++d)
+            Md->der[d][r][c] = d < nder ? DF128::coef(ders[d][2 * (r * 2 + c)], ders[d][2 * (r * 2 + c) + 1])
+                                        : DF128::coef(0, 0);
+        }
+      k_adjoint_step_mix<<<blocks, 256, 0, s>>>((double2*)psi, (double2*)lam, ngroups, bi, mask_bits(g.cbits), off,
+                                                nder, *M, *Md, part, part_stride);
+      delete Md;
+      delete M;
+      QGB_LAUNCH_CHECK("k_adjoint_step_mix");
+      return QGB_OK;
+    }
+  }
   k_adjoint_step<T, K><<<blocks, 256, 0, s>>>((S*)psi, (S*)lam, ngroups, bi, mask_bits(g.cbits), off, nder, *M,
                                              part, part_stride);
   delete M;
