@@ -1045,7 +1045,7 @@ def run_kernels(args):
             (f"Z Z expectation, {n} terms (one flip mask)", "k_expect_diag", N * S,
              lambda: check(lib.qgb_expect_pauli(st.ptr, n, code, (C.c_uint64 * n)(*zz_x), (C.c_uint64 * n)(*zz_z),
                                                 ones, n, norm.ptr, scratch, s))),
-            (f"X expectation, {x_terms} terms ({x_terms} flip masks)", "k_expect_flip", x_terms * N * S,
+            (f"X expectation, {x_terms} terms ({x_terms} flip masks)", "k_expect_flip_tile", x_terms * N * S,
              lambda: check(lib.qgb_expect_pauli(st.ptr, n, code, (C.c_uint64 * n)(*xs_x), (C.c_uint64 * n)(*xs_z),
                                                 ones, n, norm.ptr, scratch, s))),
             ("collapse on 3 qubits", "k_collapse_norm + k_collapse_apply", N * S // 8 + N * S // 8 + N * S,

@@ -18,9 +18,11 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "qgb_common.cuh"
+#include "qgb_df64.cuh"
 
 // ------------------------------------------------------------ reductions --
 __device__ __forceinline__ double warp_sum(double v) {
@@ -726,6 +728,88 @@ __global__ void __launch_bounds__(256) k_expect_flip(const typename T::S* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// Flip masks batched per tile: a CTA stages a tile of 2^L amplitudes in
+// shared memory -- index bits 0..4 and the L - 5 index bits lpos[] above
+// them, the other bits fixed by the tile -- and evaluates every term whose
+// flip mask lies inside the tile from it, so terms on up to L - 5 distinct
+// higher index bits share one read of the state instead of one pass per
+// mask.  A term adds coef (-1)^popc(i & z) Re or Im of conj(psi_i)
+// psi_{i^x} over the pairs with bit hb of i clear, as in k_expect_flip;
+// the products are formed exactly in double-float on the FP32 pipe
+// (complex128 tiles are split once on loading) and each term's tile sum is
+// flushed to FP64.
+#define FLIP_TILE_TERMS 16
+struct FlipTileSet {
+  int L;                         // a tile is 2^L amplitudes
+  int nhi;                       // local bits 5..L-1 sit at index bits lpos[0..nhi)
+  int lpos[16];
+  int nrest;                     // the index bits the tile number spreads over, ascending
+  int rest[64];
+  int nterms;
+  uint32_t xl[FLIP_TILE_TERMS];  // flip mask in local coordinates
+  int hbl[FLIP_TILE_TERMS];      // its highest local bit
+  uint32_t zl[FLIP_TILE_TERMS];  // z on the local bits, in local coordinates
+  u64 zg[FLIP_TILE_TERMS];       // z on the index (the tile's own sign)
+  double coef[FLIP_TILE_TERMS];  // c f, f = +-2 as for k_expect_flip
+  uint32_t use_im;               // bit t: Im(conj(a) b), else Re
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_expect_flip_tile(const typename T::S* __restrict__ psi, i64 ntiles,
+                                                          const __grid_constant__ FlipTileSet fs,
+                                                          double* __restrict__ part) {
+  constexpr bool C128 = T::kind == QGB_C128;
+  typedef typename std::conditional<C128, cdf, float2>::type E;
+  extern __shared__ __align__(16) unsigned char flip_smem[];
+  E* tile = reinterpret_cast<E*>(flip_smem);
+  const int M = 1 << fs.L;
+  double dsum = 0.0;
+  for (i64 tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
+    const i64 base = deposit(tt, fs.rest, fs.nrest);
+    __syncthreads();  // the previous tile is no longer read
+    for (int li = threadIdx.x; li < M; li += blockDim.x) {
+      const i64 gi = base | (li & 31) | deposit(li >> 5, fs.lpos, fs.nhi);
+      if constexpr (C128) {
+        const double2 v = psi[gi];
+        tile[li] = cdf{df_split_int(v.x), df_split_int(v.y)};
+      } else {
+        tile[li] = psi[gi];
+      }
+    }
+    __syncthreads();
+    for (int t = 0; t < fs.nterms; ++t) {
+      const uint32_t xl = fs.xl[t], zl = fs.zl[t];
+      const int hb = fs.hbl[t];
+      const uint32_t low = (1u << hb) - 1u;
+      const bool sb = __popcll((u64)base & fs.zg[t]) & 1;
+      const bool im = (fs.use_im >> t) & 1;
+      DFAcc acc{0.f, 0.f};
+      for (int p = threadIdx.x; p < (M >> 1); p += blockDim.x) {
+        const uint32_t li = (((uint32_t)p >> hb) << (hb + 1)) | ((uint32_t)p & low);
+        const E a = tile[li], b = tile[li ^ xl];
+        const bool odd = sb ^ (__popc(li & zl) & 1);
+        if constexpr (C128) {
+          // Re: a.re b.re + a.im b.im; Im: a.re b.im - a.im b.re
+          const df x[2] = {a.re, a.im};
+          const df y[2] = {im ? b.im : b.re, im ? b.re : b.im};
+          const float sx[2] = {1.f, im ? -1.f : 1.f};
+          const df r = df_dot<2>(x, y, sx);
+          acc = odd ? df_add2(acc, -r.hi, -r.lo) : df_add2(acc, r.hi, r.lo);
+        } else {
+          const float ax = odd ? -a.x : a.x, ay = odd ? -a.y : a.y;
+          const float b1 = im ? b.y : b.x, b2 = im ? b.x : b.y;
+          const float q1 = ax * b1, q2 = ay * b2;
+          acc = df_add2(acc, q1, fmaf(ax, b1, -q1));
+          acc = im ? df_add2(acc, -q2, -fmaf(ay, b2, -q2)) : df_add2(acc, q2, fmaf(ay, b2, -q2));
+        }
+      }
+      dsum += fs.coef[t] * (f2d_exact(acc.hi) + f2d_exact(acc.lo));
+    }
+  }
+  const double sum = block_sum256(dsum);
+  if (threadIdx.x == 0) part[blockIdx.x] = sum;
+}
+
 namespace {
 const int kExpectBlocksCap = 16 * 160;
 
@@ -772,7 +856,98 @@ int expect_impl(const void* state, int n, const uint64_t* xmask, const uint64_t*
   const i64 N = (i64)1 << n;
   typedef typename T::S S;
   int used = 0;
-  for (auto& pg : plan) {
+  // flip groups whose masks fit a tile (k_expect_flip_tile): batches of up
+  // to FLIP_TILE_TERMS terms on at most L - 5 distinct index bits above bit
+  // 4, one state read per batch; a batch of a single term keeps
+  // k_expect_flip
+  constexpr int L = T::kind == QGB_C128 ? 12 : 13;  // 64 KB tiles
+  std::vector<char> tiled(plan.size(), 0);
+  if (n >= L + 1) {
+    std::vector<int> cand;
+    for (size_t k = 0; k < plan.size(); ++k) {
+      const u64 x = to_index_mask(plan[k].first.x, n);
+      if (x != 0 && plan[k].first.terms.size() <= FLIP_TILE_TERMS && __builtin_popcountll(x & ~31ull) <= L - 5)
+        cand.push_back((int)k);
+    }
+    std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
+      return to_index_mask(plan[a].first.x, n) < to_index_mask(plan[b].first.x, n);
+    });
+    std::vector<std::vector<int>> batches;
+    u64 bits = 0;
+    int bterms = 0;
+    for (int k : cand) {
+      const u64 hi = to_index_mask(plan[k].first.x, n) & ~31ull;
+      const int nt = (int)plan[k].first.terms.size();
+      if (batches.empty() || __builtin_popcountll(bits | hi) > L - 5 || bterms + nt > FLIP_TILE_TERMS) {
+        batches.push_back({});
+        bits = 0;
+        bterms = 0;
+      }
+      batches.back().push_back(k);
+      bits |= hi;
+      bterms += nt;
+    }
+    for (const auto& batch : batches) {
+      int bt = 0;
+      u64 hib = 0;
+      for (int k : batch) {
+        bt += (int)plan[k].first.terms.size();
+        hib |= to_index_mask(plan[k].first.x, n) & ~31ull;
+      }
+      if (bt < 2) continue;
+      FlipTileSet* fs = new FlipTileSet();
+      memset(fs, 0, sizeof(*fs));
+      fs->L = L;
+      for (int b = 5; b < n && __builtin_popcountll(hib) < L - 5; ++b) hib |= 1ull << b;  // fill the tile
+      int local_of[64];
+      for (int b = 0; b < 64; ++b) local_of[b] = b < 5 ? b : -1;
+      for (int b = 5; b < n; ++b) {
+        if ((hib >> b) & 1) {
+          local_of[b] = 5 + fs->nhi;
+          fs->lpos[fs->nhi++] = b;
+        } else {
+          fs->rest[fs->nrest++] = b;
+        }
+      }
+      auto to_local = [&](u64 m) {
+        uint32_t r = 0;
+        for (int b = 0; b < n; ++b)
+          if (((m >> b) & 1) && local_of[b] >= 0) r |= 1u << local_of[b];
+        return r;
+      };
+      for (int k : batch) {
+        const Group& g = plan[k].first;
+        const u64 x = to_index_mask(g.x, n);
+        for (int t : g.terms) {
+          const int q = fs->nterms++;
+          const u64 z = to_index_mask(zmask[t], n);
+          const int ny = __builtin_popcountll(z & to_index_mask(xmask[t], n));
+          fs->xl[q] = to_local(x);
+          fs->hbl[q] = 31 - __builtin_clz(fs->xl[q]);
+          fs->zl[q] = to_local(z);
+          fs->zg[q] = z;
+          fs->coef[q] = coef[t] * ((ny & 3) < 2 ? 2.0 : -2.0);
+          if (ny & 1) fs->use_im |= 1u << q;
+        }
+      }
+      const i64 ntiles = (i64)1 << (n - L);
+      const int smem = (1 << L) * (T::kind == QGB_C128 ? 16 : 8);
+      int st = qgb_func_smem((const void*)k_expect_flip_tile<T>, smem);
+      if (st) {
+        delete fs;
+        return st;
+      }
+      const int blocks = (int)std::min<i64>(ntiles, std::min<i64>((i64)qgb_num_sms() * 3, kExpectBlocksCap));
+      k_expect_flip_tile<T><<<blocks, 256, smem, s>>>((const S*)state, ntiles, *fs, part + used);
+      delete fs;
+      QGB_LAUNCH_CHECK("k_expect_flip_tile");
+      used += blocks;
+      for (int k : batch) tiled[k] = 1;
+    }
+  }
+  for (size_t pk = 0; pk < plan.size(); ++pk) {
+    if (tiled[pk]) continue;
+    auto& pg = plan[pk];
     const Group& g = pg.first;
     TermSet ts;
     memset(&ts, 0, sizeof(ts));

@@ -503,6 +503,37 @@ def test_z_strings_vs_oracle(n, dtype, tol):
     assert abs(b.engine_gb.expect_pauli(st, xs, zs, coefs) - want) < tol
 
 
+@pytest.mark.parametrize("n", [16, 20])
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_flip_tiles_vs_oracle(n, dtype):
+    """X/Y terms batched per shared-memory tile (k_expect_flip_tile: states of
+    2^13 amplitudes or more, masks on up to 7 index bits above bit 4 per
+    batch): 60 random Pauli strings on 1-4 qubits plus the transverse-field
+    terms, against the oracle on the stored amplitudes, to 1e-12."""
+    from qibo_gb300.backend import GB300Backend
+    from qibo_gb300.device import DeviceState
+    from qibo_gb300.engine import pauli_masks
+
+    b = GB300Backend(dtype)
+    psi = rand_state(n, 5 + n).astype(dtype)
+    rng = np.random.default_rng(n)
+    terms, qubits, coefs = [], [], []
+    for _ in range(60):
+        k = int(rng.integers(1, 5))
+        qs = tuple(int(x) for x in rng.choice(n, k, replace=False))
+        terms.append("".join(rng.choice(list("XYZ"), k)))
+        qubits.append(qs)
+        coefs.append(float(rng.normal()))
+    for q in range(n):
+        terms.append("X")
+        qubits.append((q,))
+        coefs.append(float(rng.normal()))
+    st = DeviceState.from_numpy(psi)
+    want = ref.exp_value_observable_symbolic(psi.astype(np.complex128), terms, qubits, coefs, n)
+    xs, zs = zip(*[pauli_masks(t, q) for t, q in zip(terms, qubits)])
+    assert abs(b.engine_gb.expect_pauli(st, xs, zs, coefs) - want) < 1e-12
+
+
 @pytest.mark.parametrize("n", [12, 18])
 def test_single_term_flips_complex64(n):
     """One X or Y term per flip mask (the transverse-field terms of TFIM),
