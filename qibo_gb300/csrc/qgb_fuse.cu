@@ -67,7 +67,8 @@ void add_qubit(Block& b, int x) {
 }
 
 // U <- G U with G the op (controls all 1, targets in matrix order) embedded
-// in the block's qubit order: G applied to every column of U.
+// in the block's qubit order: G applied to every column of U, one group of
+// 2^k rows (the targets' bits over a base with the controls set) at a time.
 void apply_op(Block& b, const qgb_op& op, const double* m) {
   const int q = (int)b.qubits.size(), d = 1 << q, k = op.k, dk = 1 << k;
   auto bit_of = [&](int qubit) {
@@ -80,28 +81,34 @@ void apply_op(Block& b, const qgb_op& op, const double* m) {
     tmask |= 1 << tbit[j];
   }
   for (int j = 0; j < op.ncontrols; ++j) cmask |= 1 << bit_of(op.controls[j]);
-  std::vector<cd> col(d), out(d);
-  for (int c = 0; c < d; ++c) {
-    for (int r = 0; r < d; ++r) col[r] = b.U[(size_t)r * d + c];
-    out = col;
-    for (int base = 0; base < d; ++base) {
-      if ((base & tmask) || (base & cmask) != cmask) continue;  // group representative, controls set
-      cd in[32];
-      int idx[32];
+  int offs[32];  // row offset of target pattern a (matrix order)
+  for (int a = 0; a < dk; ++a) {
+    offs[a] = 0;
+    for (int j = 0; j < k; ++j)
+      if ((a >> (k - 1 - j)) & 1) offs[a] |= 1 << tbit[j];
+  }
+  double* U = reinterpret_cast<double*>(b.U.data());  // (re, im) pairs, row-major
+  double inr[32], ini[32];
+  for (int base = 0; base < d; ++base) {
+    if ((base & tmask) || (base & cmask) != cmask) continue;  // group representative, controls set
+    for (int c = 0; c < d; ++c) {
       for (int a = 0; a < dk; ++a) {
-        int i = base;
-        for (int j = 0; j < k; ++j)
-          if ((a >> (k - 1 - j)) & 1) i |= 1 << tbit[j];
-        idx[a] = i;
-        in[a] = col[i];
+        const double* u = U + 2 * ((size_t)(base | offs[a]) * d + c);
+        inr[a] = u[0];
+        ini[a] = u[1];
       }
       for (int r = 0; r < dk; ++r) {
-        cd acc = 0;
-        for (int a = 0; a < dk; ++a) acc += cd(m[2 * (r * dk + a)], m[2 * (r * dk + a) + 1]) * in[a];
-        out[idx[r]] = acc;
+        double ar = 0.0, ai = 0.0;
+        const double* g = m + 2 * r * dk;
+        for (int a = 0; a < dk; ++a) {
+          ar += g[2 * a] * inr[a] - g[2 * a + 1] * ini[a];
+          ai += g[2 * a] * ini[a] + g[2 * a + 1] * inr[a];
+        }
+        double* u = U + 2 * ((size_t)(base | offs[r]) * d + c);
+        u[0] = ar;
+        u[1] = ai;
       }
     }
-    for (int r = 0; r < d; ++r) b.U[(size_t)r * d + c] = out[r];
   }
 }
 
