@@ -142,7 +142,7 @@ def test_torch_autograd_surface(backend):
     e = expectation(params, c, ham, backend)
     e.backward()
     e_ref, g_ref = adjoint_gradient(backend, vqe_circuit(n, layers, p0), ham)
-    assert abs(float(e) - e_ref) < 1e-12
+    assert abs(float(e.detach()) - e_ref) < 1e-12
     np.testing.assert_allclose(params.grad.numpy(), g_ref, atol=1e-12)
 
 
