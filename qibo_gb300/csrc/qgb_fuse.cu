@@ -88,6 +88,46 @@ void apply_op(Block& b, const qgb_op& op, const double* m) {
       if ((a >> (k - 1 - j)) & 1) offs[a] |= 1 << tbit[j];
   }
   double* U = reinterpret_cast<double*>(b.U.data());  // (re, im) pairs, row-major
+  bool diag = true;
+  for (int r = 0; r < dk && diag; ++r)
+    for (int a = 0; a < dk; ++a)
+      if (a != r && (m[2 * (r * dk + a)] != 0.0 || m[2 * (r * dk + a) + 1] != 0.0)) {
+        diag = false;
+        break;
+      }
+  if (diag) {  // diagonal gates (CZ, phases): scale the rows whose entry is not 1
+    for (int a = 0; a < dk; ++a) {
+      const double gr = m[2 * (a * dk + a)], gi = m[2 * (a * dk + a) + 1];
+      if (gr == 1.0 && gi == 0.0) continue;
+      for (int base = 0; base < d; ++base) {
+        if ((base & tmask) || (base & cmask) != cmask) continue;
+        double* u = U + 2 * (size_t)(base | offs[a]) * d;
+        for (int c = 0; c < 2 * d; c += 2) {
+          const double xr = u[c], xi = u[c + 1];
+          u[c] = gr * xr - gi * xi;
+          u[c + 1] = gr * xi + gi * xr;
+        }
+      }
+    }
+    return;
+  }
+  if (dk == 2) {  // dense 1-qubit gates: an operation on two whole rows per group
+    const double g00r = m[0], g00i = m[1], g01r = m[2], g01i = m[3];
+    const double g10r = m[4], g10i = m[5], g11r = m[6], g11i = m[7];
+    for (int base = 0; base < d; ++base) {
+      if ((base & tmask) || (base & cmask) != cmask) continue;
+      double* u0 = U + 2 * (size_t)(base | offs[0]) * d;
+      double* u1 = U + 2 * (size_t)(base | offs[1]) * d;
+      for (int c = 0; c < 2 * d; c += 2) {
+        const double x0r = u0[c], x0i = u0[c + 1], x1r = u1[c], x1i = u1[c + 1];
+        u0[c] = (g00r * x0r - g00i * x0i) + (g01r * x1r - g01i * x1i);
+        u0[c + 1] = (g00r * x0i + g00i * x0r) + (g01r * x1i + g01i * x1r);
+        u1[c] = (g10r * x0r - g10i * x0i) + (g11r * x1r - g11i * x1i);
+        u1[c + 1] = (g10r * x0i + g10i * x0r) + (g11r * x1i + g11i * x1r);
+      }
+    }
+    return;
+  }
   double inr[32], ini[32];
   for (int base = 0; base < d; ++base) {
     if ((base & tmask) || (base & cmask) != cmask) continue;  // group representative, controls set
