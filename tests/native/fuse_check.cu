@@ -1,7 +1,8 @@
 // Host-side check of the engine's gate fusion (qgb_fuse5 in qgb_fuse.cu).
 //
 // Random gate lists (dense 1- and 2-qubit gates, controlled gates with up to
-// 3 controls, gates spanning more than 5 qubits that must stay unfused) are
+// 3 controls, diagonal gates with and without entries equal to 1, gates
+// spanning more than 5 qubits that must stay unfused) are
 // applied to random states of 6..10 qubits gate by gate and as the fused list
 // (every other case with padding to 5-qubit blocks);
 // the results must agree to 1e-12.  Fused ops must be uncontrolled and act on
@@ -61,9 +62,9 @@ int main() {
       std::vector<int> q(n);
       for (int j = 0; j < n; ++j) q[j] = j;
       std::shuffle(q.begin(), q.end(), rng);
-      const int kind = (int)(rng() % 10);
-      o.k = kind < 5 ? 1 : 2;
-      o.ncontrols = kind == 8 ? 1 + (int)(rng() % 3) : 0;
+      const int kind = (int)(rng() % 13);
+      o.k = kind < 5 || kind == 10 || kind == 11 ? 1 : 2;
+      o.ncontrols = kind == 8 || kind == 11 ? 1 + (int)(rng() % 3) : kind == 12 ? (int)(rng() % 2) : 0;
       if (kind == 9) {  // a gate on more than 5 qubits: 2 targets, 4 controls
         o.k = 2;
         o.ncontrols = std::min(4, n - 2);
@@ -74,7 +75,9 @@ int main() {
       const int d = 1 << o.k;
       for (int e = 0; e < d * d; ++e) {
         double re = nd(rng), im = nd(rng);
-        if (kind == 7 && (e / d != e % d)) re = im = 0;  // diagonal gates too
+        if ((kind == 7 || kind == 10 || kind == 12) && (e / d != e % d)) re = im = 0;  // diagonal gates too
+        if (kind == 10 && e == 0) re = 1.0 / 0.3, im = 0;  // a phase gate: entry (0, 0) exactly 1
+        if (kind == 12 && e / d == e % d) re = (e == d * d - 1 ? -1.0 : 1.0) / 0.3, im = 0;  // CZ, maybe controlled
         coefs.push_back(0.3 * re);
         coefs.push_back(0.3 * im);
       }
